@@ -1,0 +1,274 @@
+"""cupic_gb300: the per-step electrostatic PIC cycle of cupic on one GB300.
+
+Python mirror of the C-ABI in include/cupic_gpu.h.  ``Sim`` exposes the
+reference's host entry points under their own names (charge_deposition,
+poisson_solver, field_solver, particle_mover, cc -- src/mesh.cu,
+src/particles.cu, src/cc.cu of AntonioTejero/cupic) over the CUDA library
+``_build/libcupic_gpu.so``.  There is no CPU fallback: when the library or a
+GPU is missing, every call raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .params import Params, StepStats, workload_params
+
+__all__ = ["Sim", "Params", "StepStats", "workload_params", "load_library", "library_path",
+           "CupicError", "params_from_input_data", "SPECIES", "FLAGS", "EXPORTED"]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+SPECIES = {"electrons": 0, "ions": 1}
+FLAGS = {"cfl": 1, "capacity": 2, "stage": 4, "nonfinite": 8, "timeout": 16, "xrange": 32}
+
+# every symbol declared in include/cupic_gpu.h
+EXPORTED = [
+    "cupic_params_default", "cupic_params_from_input_data", "cupic_params_finalize",
+    "cupic_create", "cupic_destroy", "cupic_strerror", "cupic_init_plasma",
+    "cupic_load_particles", "cupic_set_time", "cupic_get_time",
+    "cupic_charge_deposition", "cupic_poisson_solver", "cupic_field_solver",
+    "cupic_particle_mover", "cupic_cc", "cupic_step", "cupic_sync",
+    "cupic_get_counts", "cupic_store_particles", "cupic_store_particles_f32",
+    "cupic_get_bookmarks", "cupic_get_rho", "cupic_get_rho_fixed", "cupic_get_phi",
+    "cupic_set_phi", "cupic_get_field", "cupic_get_phi_f32", "cupic_get_field_f32",
+    "cupic_get_stats", "cupic_get_flags", "cupic_clear_flags",
+]
+
+
+class CupicError(RuntimeError):
+    def __init__(self, status, what):
+        self.status = status
+        super().__init__(f"{what}: {strerror(status)} (status {status})")
+
+
+def library_path():
+    return os.path.join(_HERE, "_build", "libcupic_gpu.so")
+
+
+def load_library(build_if_missing=False):
+    """Load libcupic_gpu.so (built by cupic_gb300/build.py)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"{path} is missing: run `python -m cupic_gb300.build`")
+        from . import build as _b
+        _b.build()
+    L = ctypes.CDLL(path)
+    P = ctypes.POINTER
+    vp = ctypes.c_void_p
+    c_i, c_i32, c_i64, c_d = ctypes.c_int, ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+    sig = {
+        "cupic_params_default": [P(Params)],
+        "cupic_params_from_input_data": [ctypes.c_char_p, P(Params)],
+        "cupic_params_finalize": [P(Params)],
+        "cupic_create": [P(Params), c_i, P(vp)],
+        "cupic_destroy": [vp],
+        "cupic_init_plasma": [vp],
+        "cupic_load_particles": [vp, c_i, P(c_d), c_i64],
+        "cupic_set_time": [vp, c_i64, c_d, c_d, c_d],
+        "cupic_get_time": [vp, P(c_i64), P(c_d), P(c_d), P(c_d)],
+        "cupic_charge_deposition": [vp],
+        "cupic_poisson_solver": [vp, c_d, c_i32, c_i32, c_i32],
+        "cupic_field_solver": [vp],
+        "cupic_particle_mover": [vp],
+        "cupic_cc": [vp, c_d],
+        "cupic_step": [vp, c_i32],
+        "cupic_sync": [vp],
+        "cupic_get_counts": [vp, P(c_i64), P(c_i64)],
+        "cupic_store_particles": [vp, c_i, P(c_d), c_i64, P(c_i64)],
+        "cupic_store_particles_f32": [vp, c_i, P(ctypes.c_float), c_i64, P(c_i64)],
+        "cupic_get_bookmarks": [vp, c_i, P(c_i32)],
+        "cupic_get_rho": [vp, c_i, P(c_d)],
+        "cupic_get_rho_fixed": [vp, c_i, P(c_i64)],
+        "cupic_get_phi": [vp, P(c_d)],
+        "cupic_set_phi": [vp, P(c_d)],
+        "cupic_get_field": [vp, P(c_d), P(c_d)],
+        "cupic_get_phi_f32": [vp, P(ctypes.c_float)],
+        "cupic_get_field_f32": [vp, P(ctypes.c_float), P(ctypes.c_float)],
+        "cupic_get_stats": [vp, P(StepStats), c_i32],
+        "cupic_get_flags": [vp, P(ctypes.c_uint32)],
+        "cupic_clear_flags": [vp],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = c_i
+    L.cupic_strerror.argtypes = [c_i]
+    L.cupic_strerror.restype = ctypes.c_char_p
+    _LIB = L
+    return L
+
+
+def strerror(status):
+    try:
+        return load_library().cupic_strerror(status).decode()
+    except Exception:
+        return "unknown"
+
+
+def _ok(rc, what):
+    if rc != 0:
+        raise CupicError(rc, what)
+
+
+def _ptr(a, ct):
+    return a.ctypes.data_as(ctypes.POINTER(ct))
+
+
+def params_from_input_data(path):
+    """Parse the reference's input_data file (init.cu:424-789)."""
+    p = Params()
+    _ok(load_library().cupic_params_from_input_data(os.fsencode(path), ctypes.byref(p)),
+        "cupic_params_from_input_data")
+    return p
+
+
+class Sim:
+    """One plasma slab on one GPU, driven through the C-ABI."""
+
+    def __init__(self, params, device=0):
+        self.L = load_library()
+        self.p = params.copy()
+        h = ctypes.c_void_p()
+        _ok(self.L.cupic_create(ctypes.byref(self.p), device, ctypes.byref(h)), "cupic_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.cupic_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    @property
+    def nnodes(self):
+        return self.p.nnx * self.p.nny
+
+    # ---- setup ------------------------------------------------------------
+    def init_plasma(self):
+        _ok(self.L.cupic_init_plasma(self.h), "init_plasma")
+
+    def load(self, species, xyvv):
+        a = np.ascontiguousarray(xyvv, dtype=np.float64).reshape(-1, 4)
+        _ok(self.L.cupic_load_particles(self.h, species, _ptr(a, ctypes.c_double), a.shape[0]),
+            "load_particles")
+
+    def set_time(self, step, t, tin_e=-1.0, tin_i=-1.0):
+        _ok(self.L.cupic_set_time(self.h, step, t, tin_e, tin_i), "set_time")
+
+    def get_time(self):
+        s, t, a, b = ctypes.c_int64(), ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        _ok(self.L.cupic_get_time(self.h, ctypes.byref(s), ctypes.byref(t), ctypes.byref(a),
+                                  ctypes.byref(b)), "get_time")
+        return s.value, t.value, a.value, b.value
+
+    # ---- the cycle, by the reference's names --------------------------------
+    def charge_deposition(self):
+        _ok(self.L.cupic_charge_deposition(self.h), "charge_deposition")
+
+    def poisson_solver(self, max_error=None, min_sweeps=None, max_sweeps=None, check_every=1):
+        if max_error is None:
+            _ok(self.L.cupic_poisson_solver(self.h, -1.0, 0, 0, 0), "poisson_solver")
+            return
+        mn = self.p.nnx if min_sweeps is None else min_sweeps
+        mx = 1000000 if max_sweeps is None else max_sweeps
+        _ok(self.L.cupic_poisson_solver(self.h, max_error, mn, mx, check_every), "poisson_solver")
+
+    def field_solver(self):
+        _ok(self.L.cupic_field_solver(self.h), "field_solver")
+
+    def particle_mover(self):
+        _ok(self.L.cupic_particle_mover(self.h), "particle_mover")
+
+    def cc(self, t):
+        _ok(self.L.cupic_cc(self.h, t), "cc")
+
+    def step(self, n=1, sync=True):
+        _ok(self.L.cupic_step(self.h, n), "step")
+        if sync:
+            self.sync()
+
+    def sync(self):
+        _ok(self.L.cupic_sync(self.h), "sync")
+
+    # ---- results ------------------------------------------------------------
+    def counts(self):
+        a, b = ctypes.c_int64(), ctypes.c_int64()
+        _ok(self.L.cupic_get_counts(self.h, ctypes.byref(a), ctypes.byref(b)), "get_counts")
+        return a.value, b.value
+
+    def particles(self, species, f32=False):
+        n = self.counts()[species]
+        got = ctypes.c_int64()
+        if f32:
+            out = np.empty((n, 4), dtype=np.float32)
+            _ok(self.L.cupic_store_particles_f32(self.h, species, _ptr(out, ctypes.c_float), n,
+                                                 ctypes.byref(got)), "store_particles_f32")
+        else:
+            out = np.empty((n, 4), dtype=np.float64)
+            _ok(self.L.cupic_store_particles(self.h, species, _ptr(out, ctypes.c_double), n,
+                                             ctypes.byref(got)), "store_particles")
+        return out
+
+    def bookmarks(self, species):
+        out = np.empty(2 * self.p.ncy, dtype=np.int32)
+        _ok(self.L.cupic_get_bookmarks(self.h, species, _ptr(out, ctypes.c_int32)), "bookmarks")
+        return out
+
+    def row_counts(self, species):
+        bm = self.bookmarks(species).reshape(-1, 2)
+        return np.where(bm[:, 0] >= 0, bm[:, 1] - bm[:, 0] + 1, 0).astype(np.int32)
+
+    def rho(self, which=0):
+        o = np.empty(self.nnodes)
+        _ok(self.L.cupic_get_rho(self.h, which, _ptr(o, ctypes.c_double)), "get_rho")
+        return o.reshape(self.p.nny, self.p.nnx)
+
+    def rho_fixed(self, which=0):
+        o = np.empty(self.nnodes, dtype=np.int64)
+        _ok(self.L.cupic_get_rho_fixed(self.h, which, _ptr(o, ctypes.c_int64)), "get_rho_fixed")
+        return o.reshape(self.p.nny, self.p.nnx)
+
+    def phi(self):
+        o = np.empty(self.nnodes, dtype=np.float32)
+        _ok(self.L.cupic_get_phi_f32(self.h, _ptr(o, ctypes.c_float)), "get_phi")
+        return o.reshape(self.p.nny, self.p.nnx)
+
+    def set_phi(self, phi):
+        a = np.ascontiguousarray(phi, dtype=np.float64).ravel()
+        _ok(self.L.cupic_set_phi(self.h, _ptr(a, ctypes.c_double)), "set_phi")
+
+    def efield(self):
+        ex = np.empty(self.nnodes, dtype=np.float32)
+        ey = np.empty(self.nnodes, dtype=np.float32)
+        _ok(self.L.cupic_get_field_f32(self.h, _ptr(ex, ctypes.c_float), _ptr(ey, ctypes.c_float)),
+            "get_field")
+        return ex.reshape(self.p.nny, self.p.nnx), ey.reshape(self.p.nny, self.p.nnx)
+
+    def stats(self, count=1):
+        arr = (StepStats * count)()
+        _ok(self.L.cupic_get_stats(self.h, arr, count), "get_stats")
+        return [s.as_dict() for s in arr]
+
+    def flags(self):
+        f = ctypes.c_uint32()
+        _ok(self.L.cupic_get_flags(self.h, ctypes.byref(f)), "get_flags")
+        return f.value
+
+    def clear_flags(self):
+        _ok(self.L.cupic_clear_flags(self.h), "clear_flags")

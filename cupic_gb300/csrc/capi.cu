@@ -1,0 +1,940 @@
+// capi.cu -- the extern "C" entry points of libcupic_gpu.so.
+//
+// A cupic_ctx owns the device state of one plasma slab.  The stage entry
+// points mirror the reference's host functions (include/cupic_gpu.h lists
+// each with its file:line); cupic_step runs whole cycles from a captured
+// CUDA graph.  Errors are returned as CUPIC_* codes, never by exit().
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <vector>
+
+#include "cupic_internal.cuh"
+#include "kernels.h"
+
+using namespace cupic;
+
+struct cupic_ctx {
+  cupic_params p;
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  SimArgs a{};
+  Ctl *ctl = nullptr;
+  std::vector<int64_t> seg[2];
+  std::vector<int32_t> cap[2];
+  int64_t total_cap[2] = {0, 0};
+  // Jacobi geometry and exchange buffers
+  int jG = 1, jB = 1, jP = 0;
+  unsigned *jflags = nullptr;  // [G+1]: per-CTA sweep counters, then the barrier
+  float *jres = nullptr;
+  float *jhalo = nullptr;
+  // graph of one step
+  cudaGraphExec_t graph = nullptr;
+  bool graph_ok = false;
+  bool initialized = false;
+  bool rho_valid = false;
+  int host_cur = 0;
+};
+
+namespace {
+
+#define CU(call)                                   \
+  do {                                             \
+    cudaError_t e_ = (call);                       \
+    if (e_ != cudaSuccess) return cuda_status(e_); \
+  } while (0)
+
+int cuda_status(cudaError_t e) {
+  if (e == cudaErrorMemoryAllocation) {
+    cudaGetLastError();
+    return CUPIC_ERR_NOMEM;
+  }
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) return CUPIC_ERR_NODEVICE;
+  return CUPIC_ERR_CUDA;
+}
+
+template <class T>
+cudaError_t dalloc(T **p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  return cudaMalloc((void **)p, n * sizeof(T));
+}
+
+int32_t round8(double v) { return (int32_t)((((int64_t)ceil(v)) + 7) / 8 * 8); }
+
+void free_species(SpeciesDev &S) {
+  cudaFree(S.parts);
+  cudaFree(S.seg);
+  cudaFree(S.cap);
+  cudaFree(S.cnt);
+  cudaFree(S.nstay);
+  cudaFree(S.nup);
+  cudaFree(S.ndown);
+  cudaFree(S.stage_up);
+  cudaFree(S.stage_down);
+  cudaFree(S.inj_tin);
+  memset(&S, 0, sizeof(S));
+}
+
+void destroy_graph(cupic_ctx *c) {
+  if (c->graph) cudaGraphExecDestroy(c->graph);
+  c->graph = nullptr;
+  c->graph_ok = false;
+}
+
+// (Re)allocates one species with row capacities cap[j]; live counts are 0.
+int layout_species(cupic_ctx *c, int sp, const std::vector<int32_t> &capv) {
+  SpeciesDev &S = c->a.sp[sp];
+  const int ncy = c->p.ncy;
+  const int inj_cap = S.inj_cap;
+  free_species(S);
+  S.inj_cap = inj_cap;
+  c->cap[sp] = capv;
+  c->seg[sp].assign(ncy, 0);
+  int64_t tot = 0;
+  int32_t cmax = 0;
+  for (int j = 0; j < ncy; ++j) {
+    c->seg[sp][j] = tot;
+    tot += capv[j];
+    cmax = std::max(cmax, capv[j]);
+  }
+  c->total_cap[sp] = tot;
+  S.stage_cap = round8(cmax * c->p.stage_frac) + 64;
+  CU(dalloc(&S.parts, (size_t)tot));
+  CU(dalloc(&S.seg, ncy));
+  CU(dalloc(&S.cap, ncy));
+  CU(dalloc(&S.cnt, ncy));
+  CU(dalloc(&S.nstay, ncy));
+  CU(dalloc(&S.nup, ncy));
+  CU(dalloc(&S.ndown, ncy));
+  CU(dalloc(&S.stage_up, (size_t)ncy * S.stage_cap));
+  CU(dalloc(&S.stage_down, (size_t)ncy * S.stage_cap));
+  CU(dalloc(&S.inj_tin, (size_t)S.inj_cap));
+  CU(cudaMemcpy(S.seg, c->seg[sp].data(), ncy * sizeof(int64_t), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(S.cap, capv.data(), ncy * sizeof(int32_t), cudaMemcpyHostToDevice));
+  CU(cudaMemset(S.cnt, 0, ncy * sizeof(int32_t)));
+  CU(cudaMemset(S.nstay, 0, ncy * sizeof(int32_t)));
+  CU(cudaMemset(S.nup, 0, ncy * sizeof(int32_t)));
+  CU(cudaMemset(S.ndown, 0, ncy * sizeof(int32_t)));
+  destroy_graph(c);
+  return CUPIC_OK;
+}
+
+int validate(const cupic_params *p) {
+  if (!p) return CUPIC_ERR_ARG;
+  if (p->ncx < 2 || p->ncy < 2 || p->ncx > 4096 || p->ncy > (1 << 20)) return CUPIC_ERR_ARG;
+  if (!(p->ds > 0) || !(p->dt > 0) || !(p->n > 0) || !(p->eps0 > 0)) return CUPIC_ERR_ARG;
+  if (!(p->me > 0) || !(p->mi > 0) || !(p->kte > 0) || !(p->kti > 0)) return CUPIC_ERR_ARG;
+  if (p->ppr < 0 || p->max_sweeps < 0 || p->init_max_sweeps < 0) return CUPIC_ERR_ARG;
+  if (!(p->row_slack >= 0) || !(p->stage_frac > 0)) return CUPIC_ERR_ARG;
+  return CUPIC_OK;
+}
+
+void fill_constants(cupic_ctx *c) {
+  const cupic_params &p = c->p;
+  SimArgs &a = c->a;
+  a.ncx = p.ncx;
+  a.ncy = p.ncy;
+  a.nnx = p.ncx + 1;
+  a.nny = p.ncy + 1;
+  const double Lxd = p.ds * p.ncx, Lyd = p.ds * p.ncy;
+  a.ds = (float)p.ds;
+  a.inv_ds = (float)(1.0 / p.ds);
+  a.Lx = (float)Lxd;
+  a.Ly = (float)Lyd;
+  a.two_ds = (float)(2.0 * p.ds);
+  a.dt = (float)p.dt;
+  const double q[2] = {p.qe, p.qi}, m[2] = {p.me, p.mi}, kt[2] = {p.kte, p.kti};
+  for (int s = 0; s < 2; ++s) {
+    a.dtqm[s] = (float)(p.dt * q[s] / m[s]);
+    a.mhdtqm[s] = (float)(-0.5 * p.dt * q[s] / m[s]);
+    a.qm[s] = q[s] / m[s];
+    a.sig[s] = sqrt(kt[s] / m[s]);
+    /* init.cu:686-714 */
+    a.dtin[s] = sqrt(2.0 * 3.1415926535897932 * m[s] / kt[s]) / (p.n * Lxd * p.ds);
+  }
+  a.ds_d = p.ds;
+  a.inv_ds_d = 1.0 / p.ds;
+  a.Lx_d = Lxd;
+  a.Ly_d = Lyd;
+  a.dt_d = p.dt;
+  a.cb = ldexp(1.0, -32) / (p.ds * p.eps0);
+  a.ppr = p.ppr;
+  a.k0 = (uint32_t)p.seed;
+  a.k1 = (uint32_t)(p.seed >> 32);
+}
+
+int plan_jacobi(cupic_ctx *c) {
+  const int M = c->a.nny - 2, nnx = c->a.nnx;
+  int dev_max = 0;
+  CU(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+  const int P = nnx;
+  const size_t avail = (size_t)dev_max - 1024;  // static shared memory of the kernel
+  int bmax = (int)((avail / (sizeof(float) * (size_t)P) - 4) / 3);
+  if (bmax < 1) return CUPIC_ERR_ARG;
+  int G, B;
+  const char *env = getenv("CUPIC_JACOBI_CTAS");
+  const int forced = env ? atoi(env) : 0;
+  if (forced > 0) {
+    B = std::max(1, (M + forced - 1) / forced);
+  } else if (M <= bmax && (long long)M * nnx <= 65536) {
+    B = M;
+  } else {
+    B = std::max(1, (M + c->num_sms - 1) / c->num_sms);
+  }
+  B = std::min(B, bmax);
+  G = (M + B - 1) / B;
+  const size_t sm = jacobi_smem_bytes(B, P);
+  CU(jacobi_set_smem(sm));
+  int per_sm = 0;
+  CU(jacobi_max_ctas(sm, &per_sm));
+  if (per_sm < 1 || G > per_sm * c->num_sms) return CUPIC_ERR_ARG;
+  c->jG = G;
+  c->jB = B;
+  c->jP = P;
+  CU(dalloc(&c->jflags, (size_t)G + 1));
+  CU(dalloc(&c->jres, (size_t)2 * G));
+  CU(dalloc(&c->jhalo, (size_t)2 * G * 2 * P));
+  return CUPIC_OK;
+}
+
+JacobiArgs jargs(const cupic_ctx *c, double tol, int mn, int mx, int chk, int field) {
+  JacobiArgs J{};
+  J.tol = tol;
+  J.min_sweeps = mn;
+  J.max_sweeps = mx;
+  J.check_every = chk < 1 ? 1 : chk;
+  J.G = c->jG;
+  J.rows_per_cta = c->jB;
+  J.pitch = c->jP;
+  J.do_field = field;
+  J.write_stats = 1;
+  J.flags = c->jflags;
+  J.bar = c->jflags + c->jG;
+  J.res_cta = c->jres;
+  J.halo = c->jhalo;
+  return J;
+}
+
+int set_linear_phi(cupic_ctx *c) {
+  const int nnx = c->a.nnx, nny = c->a.nny;
+  std::vector<float> h((size_t)nnx * nny);
+  for (int j = 0; j < nny; ++j)
+    for (int i = 0; i < nnx; ++i)  // init.cu:235-241
+      h[(size_t)j * nnx + i] = (float)((1.0 - (double)j / (double)c->p.ncy) * c->p.phi_p);
+  CU(cudaMemcpy(c->a.phi, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return CUPIC_OK;
+}
+
+int deposit_current(cupic_ctx *c) {
+  CU(cudaMemsetAsync(c->a.rho[c->host_cur], 0,
+                     sizeof(unsigned long long) * (size_t)c->a.nnx * c->a.nny, c->stream));
+  CU(launch_deposit(c->a, c->stream));
+  c->rho_valid = true;
+  return CUPIC_OK;
+}
+
+int sync_check(cupic_ctx *c) {
+  CU(cudaStreamSynchronize(c->stream));
+  CU(cudaGetLastError());
+  return CUPIC_OK;
+}
+
+int read_ctl_flags(cupic_ctx *c, uint32_t *out) {
+  uint32_t f[2];
+  CU(cudaMemcpy(f, &c->ctl->flags, sizeof(f), cudaMemcpyDeviceToHost));
+  *out = f[0] | f[1];
+  return CUPIC_OK;
+}
+
+// status for flags raised on the device
+int flag_status(uint32_t f) {
+  if (f & CUPIC_FLAG_TIMEOUT) return CUPIC_ERR_TIMEOUT;
+  if (f & (CUPIC_FLAG_CAPACITY | CUPIC_FLAG_STAGE)) return CUPIC_ERR_CAPACITY;
+  if (f & CUPIC_FLAG_NONFINITE) return CUPIC_ERR_NONFINITE;
+  if (f & (CUPIC_FLAG_CFL | CUPIC_FLAG_XRANGE)) return CUPIC_ERR_CFL;
+  return CUPIC_OK;
+}
+
+int finish(cupic_ctx *c) {
+  int rc = sync_check(c);
+  if (rc) return rc;
+  uint32_t f = 0;
+  rc = read_ctl_flags(c, &f);
+  if (rc) return rc;
+  return flag_status(f);
+}
+
+int enqueue_step(cupic_ctx *c) {
+  const cupic_params &p = c->p;
+  CU(launch_jacobi(c->a, jargs(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1), c->stream));
+  CU(launch_zero_next_rho(c->a, c->stream));
+  CU(launch_push_deposit(c->a, c->stream));
+  CU(launch_arrive(c->a, c->stream));
+  CU(launch_inject(c->a, c->stream));
+  CU(launch_finalize(c->a, c->stream));
+  return CUPIC_OK;
+}
+
+int capture_step(cupic_ctx *c) {
+  destroy_graph(c);
+  cudaGraph_t g = nullptr;
+  CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  const int rc = enqueue_step(c);
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (rc != CUPIC_OK || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    c->graph_ok = false;
+    return CUPIC_OK;  // fall back to direct launches
+  }
+  e = cudaGraphInstantiate(&c->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    c->graph = nullptr;
+    c->graph_ok = false;
+    return CUPIC_OK;
+  }
+  c->graph_ok = true;
+  return CUPIC_OK;
+}
+
+struct PackArgs {
+  const float4 *parts;
+  const int64_t *seg;
+  const int64_t *off;  // [ncy+1] packed offsets
+  float4 *packed;
+};
+
+__global__ void k_pack(PackArgs A, int to_rows) {
+  const int j = blockIdx.x;
+  const int64_t o = A.off[j], n = A.off[j + 1] - o;
+  for (int64_t k = threadIdx.x; k < n; k += blockDim.x) {
+    if (to_rows)
+      const_cast<float4 *>(A.parts)[A.seg[j] + k] = A.packed[o + k];
+    else
+      A.packed[o + k] = A.parts[A.seg[j] + k];
+  }
+}
+
+int get_row_counts(cupic_ctx *c, int sp, std::vector<int32_t> &cnt) {
+  cnt.resize(c->p.ncy);
+  CU(cudaStreamSynchronize(c->stream));
+  CU(cudaMemcpy(cnt.data(), c->a.sp[sp].cnt, c->p.ncy * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  return CUPIC_OK;
+}
+
+// copy species sp to a packed device array, return it (caller frees)
+int pack_species(cupic_ctx *c, int sp, float4 **out, int64_t *n) {
+  std::vector<int32_t> cnt;
+  int rc = get_row_counts(c, sp, cnt);
+  if (rc) return rc;
+  const int ncy = c->p.ncy;
+  std::vector<int64_t> off(ncy + 1, 0);
+  for (int j = 0; j < ncy; ++j) off[j + 1] = off[j] + cnt[j];
+  *n = off[ncy];
+  int64_t *doff = nullptr;
+  float4 *packed = nullptr;
+  CU(dalloc(&doff, ncy + 1));
+  cudaError_t e = dalloc(&packed, (size_t)std::max<int64_t>(*n, 1));
+  if (e != cudaSuccess) {
+    cudaFree(doff);
+    return cuda_status(e);
+  }
+  CU(cudaMemcpy(doff, off.data(), (ncy + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+  PackArgs A{c->a.sp[sp].parts, c->a.sp[sp].seg, doff, packed};
+  k_pack<<<ncy, 256, 0, c->stream>>>(A, 0);
+  e = cudaStreamSynchronize(c->stream);
+  cudaFree(doff);
+  if (e != cudaSuccess) {
+    cudaFree(packed);
+    return cuda_status(e);
+  }
+  *out = packed;
+  return CUPIC_OK;
+}
+
+bool read_line(const char *path, int n, char *line, size_t cap) {
+  FILE *f = fopen(path, "r");
+  if (!f) return false;
+  bool ok = fgets(line, (int)cap, f) != nullptr;
+  for (int i = 0; ok && i < n; ++i) ok = fgets(line, (int)cap, f) != nullptr;
+  fclose(f);
+  return ok;
+}
+
+bool read_d(const char *path, int n, double *v) {
+  char line[256];
+  return read_line(path, n, line, sizeof line) && sscanf(line, "%*s = %lf;", v) == 1;
+}
+
+bool read_i(const char *path, int n, int *v) {
+  char line[256];
+  return read_line(path, n, line, sizeof line) && sscanf(line, "%*s = %d;", v) == 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *cupic_strerror(int s) {
+  switch (s) {
+    case CUPIC_OK: return "ok";
+    case CUPIC_ERR_ARG: return "invalid argument";
+    case CUPIC_ERR_CUDA: return "CUDA runtime error";
+    case CUPIC_ERR_NOMEM: return "out of memory";
+    case CUPIC_ERR_IO: return "input file could not be read";
+    case CUPIC_ERR_CAPACITY: return "row or staging capacity exceeded";
+    case CUPIC_ERR_CFL: return "a particle moved more than one cell row (or Lx) in one step";
+    case CUPIC_ERR_NONFINITE: return "non-finite particle coordinate";
+    case CUPIC_ERR_STATE: return "call out of order";
+    case CUPIC_ERR_TIMEOUT: return "a bounded device wait gave up";
+    case CUPIC_ERR_NODEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+int cupic_params_finalize(cupic_params *p) {
+  if (!p) return CUPIC_ERR_ARG;
+  const double Lx = p->ds * p->ncx;
+  p->ppr = (int32_t)(p->n * Lx * p->ds * p->ds); /* init.cu:136 */
+  return CUPIC_OK;
+}
+
+int cupic_params_default(cupic_params *p) {
+  if (!p) return CUPIC_ERR_ARG;
+  memset(p, 0, sizeof(*p));
+  p->ncx = 64;
+  p->ncy = 256;
+  p->ds = 0.5;
+  p->dt = 0.05;
+  p->n = 160.0;
+  p->eps0 = 160.0;
+  p->phi_p = -5.0;
+  p->me = 1.0;
+  p->mi = 100.0;
+  p->kte = 1.0;
+  p->kti = 1.0;
+  p->qe = -1.0;
+  p->qi = 1.0;
+  p->tol = 1e-6;
+  p->min_sweeps = 1;
+  p->max_sweeps = 2000;
+  p->check_every = 1;
+  p->init_tol = 1e-3;
+  p->init_min_sweeps = 1;
+  p->init_max_sweeps = 2000;
+  p->n_save = 100;
+  p->n_fin = 1000;
+  p->row_slack = 0.5;
+  p->stage_frac = 0.25;
+  return cupic_params_finalize(p);
+}
+
+/* read_input_file + init_* getters (init.cu:424-789): the 13 parameters
+ * are lines 1..13 after the header, each "name = value;" */
+int cupic_params_from_input_data(const char *path, cupic_params *p) {
+  if (!path || !p) return CUPIC_ERR_ARG;
+  cupic_params_default(p);
+  int n_ini, n_prev, n_save, n_fin, ncx, ncy;
+  double ne, Te, beta, gamma, phi_p, ds, dt;
+  if (!read_i(path, 1, &n_ini) || !read_i(path, 2, &n_prev) || !read_i(path, 3, &n_save) ||
+      !read_i(path, 4, &n_fin) || !read_d(path, 5, &ne) || !read_d(path, 6, &Te) ||
+      !read_d(path, 7, &beta) || !read_d(path, 8, &gamma) || !read_d(path, 9, &phi_p) ||
+      !read_i(path, 10, &ncx) || !read_i(path, 11, &ncy) || !read_d(path, 12, &ds) ||
+      !read_d(path, 13, &dt))
+    return CUPIC_ERR_IO;
+  const double ME = 9.109e-31, E = 1.602e-19, KB = 1.381e-23, EPS = 8.854e-12; /* init.h:24-27 */
+  const double Dl = sqrt(EPS * KB * Te / (ne * E * E));                       /* init.cu:729 */
+  double n = ne;
+  n *= Dl * Dl * Dl; /* init.cu:552 */
+  double eps = EPS;  /* init.cu:622-626 */
+  eps /= pow(Dl * sqrt(ME / (KB * Te)), 2);
+  eps /= E * E;
+  eps *= Dl * Dl * Dl;
+  eps *= ME;
+  double php = phi_p;
+  php *= E / (KB * Te); /* init.cu:534 */
+  p->n_ini = n_ini;
+  p->n_prev = n_prev;
+  p->n_save = n_save;
+  p->n_fin = n_fin;
+  p->ncx = ncx;
+  p->ncy = ncy;
+  p->ds = ds;
+  p->dt = dt;
+  p->n = n;
+  p->eps0 = eps;
+  p->phi_p = php;
+  p->mi = gamma;
+  p->kti = beta;
+  const int mn = std::max(ncx + 1, ncy + 1) + 1; /* mesh.cu:67,94: sweeps >= max(nnx,nny)+1 */
+  p->tol = 1e-4;                                 /* main.cu:64 */
+  p->min_sweeps = mn;
+  p->max_sweeps = 1000000;
+  p->check_every = 1;
+  p->init_tol = 1e-3; /* init.cu:254 */
+  p->init_min_sweeps = mn;
+  p->init_max_sweeps = 1000000;
+  return cupic_params_finalize(p);
+}
+
+int cupic_create(const cupic_params *pin, int device, cupic_ctx **out) {
+  if (!out) return CUPIC_ERR_ARG;
+  *out = nullptr;
+  int rc = validate(pin);
+  if (rc) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return CUPIC_ERR_NODEVICE;
+  }
+  if (device < 0 || device >= ndev) return CUPIC_ERR_ARG;
+  cupic_ctx *c = new (std::nothrow) cupic_ctx();
+  if (!c) return CUPIC_ERR_NOMEM;
+  c->p = *pin;
+  c->device = device;
+  auto fail = [&](int r) {
+    cupic_destroy(c);
+    return r;
+  };
+  if (cudaSetDevice(device) != cudaSuccess) return fail(CUPIC_ERR_CUDA);
+  if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+    return fail(CUPIC_ERR_CUDA);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return fail(CUPIC_ERR_CUDA);
+  fill_constants(c);
+  SimArgs &a = c->a;
+  const size_t nodes = (size_t)a.nnx * a.nny;
+  if (dalloc(&a.phi, nodes) || dalloc(&a.E, nodes) || dalloc(&a.rho[0], nodes) ||
+      dalloc(&a.rho[1], nodes) || dalloc(&c->ctl, 1))
+    return fail(CUPIC_ERR_NOMEM);
+  a.ctl = c->ctl;
+  if (cudaMemset(a.phi, 0, nodes * sizeof(float)) || cudaMemset(a.E, 0, nodes * sizeof(float2)) ||
+      cudaMemset(a.rho[0], 0, nodes * 8) || cudaMemset(a.rho[1], 0, nodes * 8) ||
+      cudaMemset(c->ctl, 0, sizeof(Ctl)))
+    return fail(CUPIC_ERR_CUDA);
+  const int32_t capj = round8(c->p.ppr * (1.0 + c->p.row_slack)) + 64;
+  for (int sp = 0; sp < 2; ++sp) {
+    const double per_step = c->p.dt / a.dtin[sp];
+    a.sp[sp].inj_cap = (int32_t)std::min(4.0 * ceil(per_step) + 1024.0, 1.0e8);
+    rc = layout_species(c, sp, std::vector<int32_t>(c->p.ncy, capj));
+    if (rc) return fail(rc);
+  }
+  rc = plan_jacobi(c);
+  if (rc) return fail(rc);
+  if (push_set_smem(push_smem_bytes(a.nnx)) != cudaSuccess) return fail(CUPIC_ERR_ARG);
+  rc = cupic_set_time(c, (int64_t)c->p.n_ini + 1, c->p.n_ini * c->p.dt + c->p.dt, -1.0, -1.0);
+  if (rc) return fail(rc);
+  *out = c;
+  return CUPIC_OK;
+}
+
+int cupic_destroy(cupic_ctx *c) {
+  if (!c) return CUPIC_ERR_ARG;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  destroy_graph(c);
+  for (int sp = 0; sp < 2; ++sp) free_species(c->a.sp[sp]);
+  cudaFree(c->a.phi);
+  cudaFree(c->a.E);
+  cudaFree(c->a.rho[0]);
+  cudaFree(c->a.rho[1]);
+  cudaFree(c->ctl);
+  cudaFree(c->jflags);
+  cudaFree(c->jres);
+  cudaFree(c->jhalo);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return CUPIC_OK;
+}
+
+int cupic_set_time(cupic_ctx *c, int64_t step, double t, double tin_e, double tin_i) {
+  if (!c) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  CU(cudaStreamSynchronize(c->stream));
+  struct {
+    int64_t step;
+    double t;
+    double tin[2];
+    int32_t tin_set[2];
+  } h = {step, t, {tin_e, tin_i}, {tin_e >= 0 ? 1 : 0, tin_i >= 0 ? 1 : 0}};
+  static_assert(sizeof(h) == offsetof(Ctl, cur), "Ctl layout");
+  CU(cudaMemcpy(c->ctl, &h, sizeof(h), cudaMemcpyHostToDevice));
+  return CUPIC_OK;
+}
+
+int cupic_get_time(cupic_ctx *c, int64_t *step, double *t, double *tin_e, double *tin_i) {
+  if (!c) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  CU(cudaStreamSynchronize(c->stream));
+  struct {
+    int64_t step;
+    double t;
+    double tin[2];
+    int32_t tin_set[2];
+  } h;
+  CU(cudaMemcpy(&h, c->ctl, sizeof(h), cudaMemcpyDeviceToHost));
+  if (step) *step = h.step;
+  if (t) *t = h.t;
+  if (tin_e) *tin_e = h.tin_set[0] ? h.tin[0] : -1.0;
+  if (tin_i) *tin_i = h.tin_set[1] ? h.tin[1] : -1.0;
+  return CUPIC_OK;
+}
+
+int cupic_init_plasma(cupic_ctx *c) {
+  if (!c) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  const int capj = c->cap[0].empty() ? 0 : *std::min_element(c->cap[0].begin(), c->cap[0].end());
+  if (capj < c->p.ppr) return CUPIC_ERR_CAPACITY;
+  CU(launch_init_particles(c->a, c->stream));
+  int rc = set_linear_phi(c);
+  if (rc) return rc;
+  rc = deposit_current(c);
+  if (rc) return rc;
+  const cupic_params &p = c->p;
+  CU(launch_jacobi(c->a, jargs(c, p.init_tol, p.init_min_sweeps, p.init_max_sweeps, p.check_every, 1),
+                   c->stream));
+  CU(launch_leapfrog_start(c->a, c->stream));
+  rc = sync_check(c);
+  if (rc) return rc;
+  rc = cupic_set_time(c, (int64_t)p.n_ini + 1, p.n_ini * p.dt + p.dt, -1.0, -1.0);
+  if (rc) return rc;
+  c->initialized = true;
+  return finish(c);
+}
+
+int cupic_load_particles(cupic_ctx *c, int sp, const double *xyvv, int64_t n) {
+  if (!c || sp < 0 || sp > 1 || n < 0 || (n > 0 && !xyvv)) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  const int ncy = c->p.ncy;
+  const float inv_ds = c->a.inv_ds, Lx = c->a.Lx, Ly = c->a.Ly;
+  std::vector<int32_t> cnt(ncy, 0);
+  std::vector<int32_t> rowk((size_t)n);
+  for (int64_t k = 0; k < n; ++k) {
+    const float x = (float)xyvv[4 * k], y = (float)xyvv[4 * k + 1];
+    if (!(x >= 0.0f && x < Lx && y >= 0.0f && y < Ly)) return CUPIC_ERR_ARG;
+    const float sy = y * inv_ds;
+    int j = (int)floorf(sy);
+    j = j < 0 ? 0 : (j > ncy - 1 ? ncy - 1 : j);
+    rowk[k] = j;
+    cnt[j]++;
+  }
+  std::vector<int64_t> off(ncy + 1, 0);
+  for (int j = 0; j < ncy; ++j) off[j + 1] = off[j] + cnt[j];
+  std::vector<float4> packed((size_t)std::max<int64_t>(n, 1));
+  std::vector<int64_t> fill(off.begin(), off.end() - 1);
+  for (int64_t k = 0; k < n; ++k) {
+    packed[fill[rowk[k]]++] = make_float4((float)xyvv[4 * k], (float)xyvv[4 * k + 1],
+                                          (float)xyvv[4 * k + 2], (float)xyvv[4 * k + 3]);
+  }
+  bool grow = false;
+  std::vector<int32_t> capv = c->cap[sp];
+  for (int j = 0; j < ncy; ++j)
+    if (cnt[j] > capv[j]) {
+      capv[j] = round8(cnt[j] * (1.0 + c->p.row_slack)) + 64;
+      grow = true;
+    }
+  CU(cudaStreamSynchronize(c->stream));
+  if (grow) {
+    int rc = layout_species(c, sp, capv);
+    if (rc) return rc;
+  }
+  SpeciesDev &S = c->a.sp[sp];
+  int64_t *doff = nullptr;
+  float4 *dp = nullptr;
+  CU(dalloc(&doff, ncy + 1));
+  CU(dalloc(&dp, packed.size()));
+  CU(cudaMemcpy(doff, off.data(), (ncy + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(dp, packed.data(), packed.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  PackArgs A{S.parts, S.seg, doff, dp};
+  k_pack<<<ncy, 256, 0, c->stream>>>(A, 1);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(S.cnt, cnt.data(), ncy * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  cudaFree(doff);
+  cudaFree(dp);
+  c->rho_valid = false;
+  c->initialized = true;
+  return CUPIC_OK;
+}
+
+int cupic_charge_deposition(cupic_ctx *c) {
+  if (!c) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  int rc = deposit_current(c);
+  if (rc) return rc;
+  return sync_check(c);
+}
+
+int cupic_poisson_solver(cupic_ctx *c, double max_error, int32_t mn, int32_t mx, int32_t chk) {
+  if (!c) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  if (!c->rho_valid) {
+    int rc = deposit_current(c);
+    if (rc) return rc;
+  }
+  if (max_error < 0) {
+    max_error = c->p.tol;
+    mn = c->p.min_sweeps;
+    mx = c->p.max_sweeps;
+    chk = c->p.check_every;
+  }
+  if (mx < 0) return CUPIC_ERR_ARG;
+  CU(launch_jacobi(c->a, jargs(c, max_error, mn, mx, chk, 0), c->stream));
+  return finish(c);
+}
+
+int cupic_field_solver(cupic_ctx *c) {
+  if (!c) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  JacobiArgs J = jargs(c, 0.0, 0, 0, 1, 1);
+  J.write_stats = 0;
+  CU(launch_jacobi(c->a, J, c->stream));
+  return finish(c);
+}
+
+int cupic_particle_mover(cupic_ctx *c) {
+  if (!c) return CUPIC_ERR_ARG;
+  if (!c->initialized) return CUPIC_ERR_STATE;
+  CU(cudaSetDevice(c->device));
+  CU(launch_zero_next_rho(c->a, c->stream));
+  CU(launch_push_deposit(c->a, c->stream));
+  CU(launch_arrive(c->a, c->stream));
+  return finish(c);
+}
+
+int cupic_cc(cupic_ctx *c, double t) {
+  if (!c) return CUPIC_ERR_ARG;
+  if (!c->initialized) return CUPIC_ERR_STATE;
+  CU(cudaSetDevice(c->device));
+  CU(cudaStreamSynchronize(c->stream));
+  CU(cudaMemcpy(&c->ctl->t, &t, sizeof(double), cudaMemcpyHostToDevice));
+  CU(launch_inject(c->a, c->stream));
+  CU(launch_finalize(c->a, c->stream));
+  c->host_cur ^= 1;
+  c->rho_valid = true;
+  return finish(c);
+}
+
+int cupic_step(cupic_ctx *c, int32_t nsteps) {
+  if (!c || nsteps < 0) return CUPIC_ERR_ARG;
+  if (!c->initialized) return CUPIC_ERR_STATE;
+  CU(cudaSetDevice(c->device));
+  if (!c->rho_valid) {
+    int rc = deposit_current(c);
+    if (rc) return rc;
+  }
+  if (!c->graph_ok) {
+    int rc = capture_step(c);
+    if (rc) return rc;
+  }
+  for (int i = 0; i < nsteps; ++i) {
+    if (c->graph_ok) {
+      CU(cudaGraphLaunch(c->graph, c->stream));
+    } else {
+      int rc = enqueue_step(c);
+      if (rc) return rc;
+    }
+    c->host_cur ^= 1;
+  }
+  return CUPIC_OK;
+}
+
+int cupic_sync(cupic_ctx *c) {
+  if (!c) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  return finish(c);
+}
+
+int cupic_get_counts(cupic_ctx *c, int64_t *ne, int64_t *ni) {
+  if (!c) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  for (int sp = 0; sp < 2; ++sp) {
+    std::vector<int32_t> cnt;
+    int rc = get_row_counts(c, sp, cnt);
+    if (rc) return rc;
+    int64_t s = 0;
+    for (int32_t v : cnt) s += v;
+    if (sp == 0 && ne) *ne = s;
+    if (sp == 1 && ni) *ni = s;
+  }
+  return CUPIC_OK;
+}
+
+int cupic_store_particles_f32(cupic_ctx *c, int sp, float *out, int64_t capacity, int64_t *n_out) {
+  if (!c || sp < 0 || sp > 1) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  float4 *packed = nullptr;
+  int64_t n = 0;
+  int rc = pack_species(c, sp, &packed, &n);
+  if (rc) return rc;
+  if (n_out) *n_out = n;
+  if (n > capacity || (n > 0 && !out)) {
+    cudaFree(packed);
+    return CUPIC_ERR_ARG;
+  }
+  cudaError_t e = cudaMemcpy(out, packed, (size_t)n * sizeof(float4), cudaMemcpyDeviceToHost);
+  cudaFree(packed);
+  return e == cudaSuccess ? CUPIC_OK : cuda_status(e);
+}
+
+int cupic_store_particles(cupic_ctx *c, int sp, double *out, int64_t capacity, int64_t *n_out) {
+  if (!c || sp < 0 || sp > 1) return CUPIC_ERR_ARG;
+  int64_t ne = 0, ni = 0;
+  int rc = cupic_get_counts(c, &ne, &ni);
+  if (rc) return rc;
+  const int64_t n = sp == 0 ? ne : ni;
+  if (n_out) *n_out = n;
+  if (n > capacity || (n > 0 && !out)) return CUPIC_ERR_ARG;
+  std::vector<float> tmp((size_t)std::max<int64_t>(4 * n, 4));
+  int64_t got = 0;
+  rc = cupic_store_particles_f32(c, sp, tmp.data(), n, &got);
+  if (rc) return rc;
+  for (int64_t k = 0; k < 4 * got; ++k) out[k] = (double)tmp[k];
+  return CUPIC_OK;
+}
+
+int cupic_get_bookmarks(cupic_ctx *c, int sp, int32_t *bm) {
+  if (!c || sp < 0 || sp > 1 || !bm) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  std::vector<int32_t> cnt;
+  int rc = get_row_counts(c, sp, cnt);
+  if (rc) return rc;
+  int64_t off = 0;
+  for (int j = 0; j < c->p.ncy; ++j) {
+    if (cnt[j] > 0) {
+      bm[2 * j] = (int32_t)off;
+      bm[2 * j + 1] = (int32_t)(off + cnt[j] - 1);
+    } else {
+      bm[2 * j] = bm[2 * j + 1] = -1;
+    }
+    off += cnt[j];
+  }
+  return CUPIC_OK;
+}
+
+int cupic_get_rho_fixed(cupic_ctx *c, int which, int64_t *acc) {
+  if (!c || !acc || which < 0 || which > 1) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  if (which == 0 && !c->rho_valid) {
+    int rc = deposit_current(c);
+    if (rc) return rc;
+  }
+  CU(cudaStreamSynchronize(c->stream));
+  const size_t nodes = (size_t)c->a.nnx * c->a.nny;
+  CU(cudaMemcpy(acc, c->a.rho[c->host_cur ^ which], nodes * sizeof(int64_t), cudaMemcpyDeviceToHost));
+  return CUPIC_OK;
+}
+
+int cupic_get_rho(cupic_ctx *c, int which, double *rho) {
+  if (!c || !rho) return CUPIC_ERR_ARG;
+  const int nnx = c->a.nnx, nny = c->a.nny;
+  std::vector<int64_t> acc((size_t)nnx * nny);
+  int rc = cupic_get_rho_fixed(c, which, acc.data());
+  if (rc) return rc;
+  const double ds3 = c->p.ds * c->p.ds * c->p.ds, scale = ldexp(1.0, -32);
+  for (int j = 0; j < nny; ++j) {
+    const double vol = (j == 0 || j == nny - 1) ? 0.5 * ds3 : ds3;
+    const size_t r = (size_t)j * nnx;
+    for (int i = 0; i < nnx; ++i) {
+      const int64_t f = (i == 0 || i == nnx - 1) ? acc[r] + acc[r + nnx - 1] : acc[r + i];
+      rho[r + i] = (double)f * scale / vol;
+    }
+  }
+  return CUPIC_OK;
+}
+
+int cupic_get_phi_f32(cupic_ctx *c, float *phi) {
+  if (!c || !phi) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  CU(cudaStreamSynchronize(c->stream));
+  CU(cudaMemcpy(phi, c->a.phi, sizeof(float) * (size_t)c->a.nnx * c->a.nny, cudaMemcpyDeviceToHost));
+  return CUPIC_OK;
+}
+
+int cupic_get_phi(cupic_ctx *c, double *phi) {
+  if (!c || !phi) return CUPIC_ERR_ARG;
+  std::vector<float> h((size_t)c->a.nnx * c->a.nny);
+  int rc = cupic_get_phi_f32(c, h.data());
+  if (rc) return rc;
+  for (size_t k = 0; k < h.size(); ++k) phi[k] = (double)h[k];
+  return CUPIC_OK;
+}
+
+int cupic_set_phi(cupic_ctx *c, const double *phi) {
+  if (!c || !phi) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  std::vector<float> h((size_t)c->a.nnx * c->a.nny);
+  for (size_t k = 0; k < h.size(); ++k) h[k] = (float)phi[k];
+  CU(cudaStreamSynchronize(c->stream));
+  CU(cudaMemcpy(c->a.phi, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return CUPIC_OK;
+}
+
+int cupic_get_field_f32(cupic_ctx *c, float *ex, float *ey) {
+  if (!c || !ex || !ey) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  CU(cudaStreamSynchronize(c->stream));
+  const size_t nodes = (size_t)c->a.nnx * c->a.nny;
+  std::vector<float2> h(nodes);
+  CU(cudaMemcpy(h.data(), c->a.E, nodes * sizeof(float2), cudaMemcpyDeviceToHost));
+  for (size_t k = 0; k < nodes; ++k) {
+    ex[k] = h[k].x;
+    ey[k] = h[k].y;
+  }
+  return CUPIC_OK;
+}
+
+int cupic_get_field(cupic_ctx *c, double *ex, double *ey) {
+  if (!c || !ex || !ey) return CUPIC_ERR_ARG;
+  const size_t nodes = (size_t)c->a.nnx * c->a.nny;
+  std::vector<float> hx(nodes), hy(nodes);
+  int rc = cupic_get_field_f32(c, hx.data(), hy.data());
+  if (rc) return rc;
+  for (size_t k = 0; k < nodes; ++k) {
+    ex[k] = hx[k];
+    ey[k] = hy[k];
+  }
+  return CUPIC_OK;
+}
+
+int cupic_get_stats(cupic_ctx *c, cupic_step_stats *out, int32_t count) {
+  if (!c || !out || count < 0 || count > kStatsRing) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  CU(cudaStreamSynchronize(c->stream));
+  int64_t step = 0;
+  CU(cudaMemcpy(&step, &c->ctl->step, sizeof(step), cudaMemcpyDeviceToHost));
+  for (int32_t k = 0; k < count; ++k) {
+    const int64_t s = step - count + k;
+    const int64_t idx = ((s % kStatsRing) + kStatsRing) % kStatsRing;
+    CU(cudaMemcpy(&out[k], &c->ctl->ring[idx], sizeof(cupic_step_stats), cudaMemcpyDeviceToHost));
+  }
+  return CUPIC_OK;
+}
+
+int cupic_get_flags(cupic_ctx *c, uint32_t *flags) {
+  if (!c || !flags) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  CU(cudaStreamSynchronize(c->stream));
+  return read_ctl_flags(c, flags);
+}
+
+int cupic_clear_flags(cupic_ctx *c) {
+  if (!c) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  CU(cudaStreamSynchronize(c->stream));
+  uint32_t z[2] = {0u, 0u};
+  int32_t zero = 0;
+  CU(cudaMemcpy(&c->ctl->flags, z, sizeof(z), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(&c->ctl->abort, &zero, sizeof(zero), cudaMemcpyHostToDevice));
+  return CUPIC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,263 @@
+// cupic_internal.cuh -- device-side state layout and per-particle arithmetic
+// of the GB300 PIC cycle.  Every floating-point operation here rounds where
+// the source says: the library is compiled with -fmad=false and uses
+// explicit __fmaf_rn / __fma_rn where a fused multiply-add is intended, so
+// the CPU oracle can reproduce each result bit for bit.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/cupic_gpu.h"
+
+namespace cupic {
+
+constexpr int kRowAbsorbed = -1;
+constexpr int kRowRemoved = -2;
+constexpr int kStatsRing = 4096;      // per-step stats kept on the device
+constexpr int kPurposeInit = 0;       // Philox counter word 3, bits 8..15
+constexpr int kPurposeInject = 1;
+
+// Control block resident in device memory; the kernels of a step read and
+// advance it, so a captured graph of one step can be replayed unchanged.
+struct Ctl {
+  int64_t step;           // index i of the next step (main.cu:59)
+  double t;               // time passed to the boundary stage of that step
+  double tin[2];          // next injection time per species (cc.cu:35-36)
+  int32_t tin_set[2];     // 0 until the first boundary call
+  int32_t cur;            // rho[cur] holds the charge of the current particles
+  uint32_t flags;         // sticky CUPIC_FLAG_* bits
+  uint32_t step_flags;    // flags raised during the current step
+  int32_t sweeps;         // Jacobi sweeps of the last solve
+  float residual;         // max |dphi| of its last checked sweep
+  int32_t inj_count[2];   // injected this step
+  unsigned long long absorbed[2];
+  unsigned long long removed[2];
+  int32_t abort;          // a bounded wait gave up: kernels bail out
+  int32_t pad;
+  cupic_step_stats ring[kStatsRing];
+};
+
+// Per-species particle storage: rows are contiguous segments of `parts`
+// with fixed capacity; the live prefix of row j is [seg[j], seg[j]+cnt[j]).
+struct SpeciesDev {
+  float4 *parts;          // {x, y, vx, vy}
+  int64_t *seg;           // [ncy] segment start
+  int32_t *cap;           // [ncy] segment capacity
+  int32_t *cnt;           // [ncy] live particles
+  int32_t *nstay;         // [ncy] stayed in the row this step
+  int32_t *nup;           // [ncy] moved to row+1 (staged in stage_up)
+  int32_t *ndown;         // [ncy] moved to row-1 (staged in stage_down)
+  float4 *stage_up;       // [ncy * stage_cap]
+  float4 *stage_down;     // [ncy * stage_cap]
+  int32_t stage_cap;
+  int32_t inj_cap;        // most particles injected per step
+  double *inj_tin;        // [inj_cap] scratch: injection time of each draw
+};
+
+// Everything a kernel needs, passed by value.
+struct SimArgs {
+  int ncx, ncy, nnx, nny;
+  // single-precision constants, each rounded once from double
+  float ds, inv_ds, Lx, Ly, two_ds, dt;
+  float dtqm[2], mhdtqm[2];
+  // double-precision constants (injection, charge conversion)
+  double ds_d, inv_ds_d, Lx_d, Ly_d, dt_d;
+  double cb;              // fixed-point charge -> Jacobi source term
+  double dtin[2], qm[2], sig[2];
+  int32_t ppr;
+  uint32_t k0, k1;        // generator key (seed)
+  SpeciesDev sp[2];
+  float *phi;             // [nny*nnx]
+  float2 *E;              // [nny*nnx] {Ex, Ey}
+  unsigned long long *rho[2];  // raw (unfolded) fixed-point charge, 2^32 per unit
+  Ctl *ctl;
+};
+
+// Jacobi launch description (see jacobi.cu).
+struct JacobiArgs {
+  double tol;
+  int32_t min_sweeps, max_sweeps, check_every;
+  int32_t G;              // CTAs (cooperative)
+  int32_t rows_per_cta;   // interior rows owned by one CTA (last may own fewer)
+  int32_t pitch;          // smem row pitch in floats
+  int32_t do_field;       // 1: derive E after the last sweep
+  int32_t write_stats;    // 1: store sweeps/residual in the control block
+  unsigned int *flags;    // [G] last sweep published by each CTA
+  unsigned int *bar;      // [1] grid barrier counter
+  float *res_cta;         // [2*G] per-CTA max |dphi| of a checked sweep
+  float *halo;            // [2 parity][G][2 rows][pitch]
+};
+
+// ---------------------------------------------------------------------------
+// arithmetic shared by the kernels
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float clamp01f(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
+__device__ __forceinline__ double clamp01d(double v) { return fmin(fmax(v, 0.0), 1.0); }
+
+// floor(v) clamped to [lo, hi]; NaN -> lo
+__device__ __forceinline__ int cfloorf(float v, int lo, int hi) {
+  if (!(v >= (float)lo)) return lo;
+  if (v >= (float)(hi + 1)) return hi;
+  int i = (int)floorf(v);
+  return i > hi ? hi : i;
+}
+__device__ __forceinline__ int cfloord(double v, int lo, int hi) {
+  if (!(v >= (double)lo)) return lo;
+  if (v >= (double)(hi + 1)) return hi;
+  int i = (int)floor(v);
+  return i > hi ? hi : i;
+}
+
+__device__ __forceinline__ int row_of(const SimArgs &a, float y) {
+  return cfloorf(__fmul_rn(y, a.inv_ds), 0, a.ncy - 1);
+}
+
+// periodic x: [0, Lx), applied as two sequential tests so that a tiny
+// negative x that rounds to Lx after +Lx ends at 0
+__device__ __forceinline__ float wrap_x(const SimArgs &a, float x) {
+  if (x < 0.0f) x = __fadd_rn(x, a.Lx);
+  if (x >= a.Lx) x = __fsub_rn(x, a.Lx);
+  return x;
+}
+
+// Philox4x32-10 (Salmon et al., SC'11)
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+    const uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+__device__ __forceinline__ double u01(uint32_t r) { return ((double)r + 0.5) * 0x1p-32; }
+
+// natural log from IEEE basic operations (exponent split, atanh series)
+__device__ __forceinline__ double dev_log(double x) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  int e = (int)((b >> 52) & 0x7ff) - 1023;
+  b = (b & 0x000fffffffffffffull) | 0x3ff0000000000000ull;
+  double m = __longlong_as_double((long long)b);
+  if (m > 1.4142135623730951) {
+    m = m * 0.5;
+    e += 1;
+  }
+  const double s = (m - 1.0) / (m + 1.0);
+  const double s2 = s * s;
+  double q = 1.0 / 23.0;
+  q = q * s2 + 1.0 / 21.0;
+  q = q * s2 + 1.0 / 19.0;
+  q = q * s2 + 1.0 / 17.0;
+  q = q * s2 + 1.0 / 15.0;
+  q = q * s2 + 1.0 / 13.0;
+  q = q * s2 + 1.0 / 11.0;
+  q = q * s2 + 1.0 / 9.0;
+  q = q * s2 + 1.0 / 7.0;
+  q = q * s2 + 1.0 / 5.0;
+  q = q * s2 + 1.0 / 3.0;
+  q = q * s2 + 1.0;
+  return (double)e * 0.69314718055994531 + 2.0 * s * q;
+}
+
+// sin, cos of th in [0, pi/4], Taylor series to th^17 / th^16
+__device__ __forceinline__ void dev_sincos_small(double th, double *s, double *c) {
+  const double t2 = th * th;
+  double ps = -1.0 / 355687428096000.0;
+  ps = ps * t2 + 1.0 / 1307674368000.0;
+  ps = ps * t2 - 1.0 / 6227020800.0;
+  ps = ps * t2 + 1.0 / 39916800.0;
+  ps = ps * t2 - 1.0 / 362880.0;
+  ps = ps * t2 + 1.0 / 5040.0;
+  ps = ps * t2 - 1.0 / 120.0;
+  ps = ps * t2 + 1.0 / 6.0;
+  *s = th - th * t2 * ps;
+  double pc = 1.0 / 20922789888000.0;
+  pc = pc * t2 - 1.0 / 87178291200.0;
+  pc = pc * t2 + 1.0 / 479001600.0;
+  pc = pc * t2 - 1.0 / 3628800.0;
+  pc = pc * t2 + 1.0 / 40320.0;
+  pc = pc * t2 - 1.0 / 720.0;
+  pc = pc * t2 + 1.0 / 24.0;
+  pc = pc * t2 - 0.5;
+  *c = 1.0 + t2 * pc;
+}
+
+// sin(2 pi u), cos(2 pi u), u in [0,1), by octant reduction
+__device__ __forceinline__ void dev_sincos2pi(double u, double *s, double *c) {
+  const double r = u * 8.0;
+  int o = (int)r;
+  o = o > 7 ? 7 : (o < 0 ? 0 : o);
+  const double f = r - (double)o;
+  const double qpi = 0.78539816339744831;
+  double sa, ca;
+  dev_sincos_small(((o & 1) ? (1.0 - f) : f) * qpi, &sa, &ca);
+  switch (o) {
+    case 0: *s = sa; *c = ca; break;
+    case 1: *s = ca; *c = sa; break;
+    case 2: *s = ca; *c = -sa; break;
+    case 3: *s = sa; *c = -ca; break;
+    case 4: *s = -sa; *c = -ca; break;
+    case 5: *s = -ca; *c = -sa; break;
+    case 6: *s = -ca; *c = sa; break;
+    default: *s = -sa; *c = ca; break;
+  }
+}
+
+// CIC field at a particle of cell row s, from a shared tile holding node
+// rows s and s+1 (tile row stride = nnx).
+__device__ __forceinline__ void gather_tile(const SimArgs &a, const float2 *tile, float x, float y,
+                                            int s, float &Epx, float &Epy) {
+  const float sx = __fmul_rn(x, a.inv_ds);
+  const int ic = cfloorf(sx, 0, a.ncx - 1);
+  const float fx = clamp01f(__fsub_rn(sx, (float)ic));
+  const float fy = clamp01f(__fsub_rn(__fmul_rn(y, a.inv_ds), (float)s));
+  const float gx = __fsub_rn(1.0f, fx), gy = __fsub_rn(1.0f, fy);
+  const float w00 = __fmul_rn(gx, gy), w10 = __fmul_rn(fx, gy);
+  const float w01 = __fmul_rn(gx, fy), w11 = __fmul_rn(fx, fy);
+  const float2 e00 = tile[ic], e10 = tile[ic + 1];
+  const float2 e01 = tile[a.nnx + ic], e11 = tile[a.nnx + ic + 1];
+  float ex = __fmul_rn(w00, e00.x);
+  ex = __fmaf_rn(w10, e10.x, ex);
+  ex = __fmaf_rn(w01, e01.x, ex);
+  ex = __fmaf_rn(w11, e11.x, ex);
+  float ey = __fmul_rn(w00, e00.y);
+  ey = __fmaf_rn(w10, e10.y, ey);
+  ey = __fmaf_rn(w01, e01.y, ey);
+  ey = __fmaf_rn(w11, e11.y, ey);
+  Epx = ex;
+  Epy = ey;
+}
+
+// fixed-point CIC weights (16 fractional bits per axis, 2^32 per particle)
+struct CicFixed {
+  int ic, jc;
+  long long w00, w10, w01, w11;
+};
+
+__device__ __forceinline__ CicFixed cic_fixed(const SimArgs &a, float x, float y) {
+  CicFixed r;
+  const float sx = __fmul_rn(x, a.inv_ds);
+  r.ic = cfloorf(sx, 0, a.ncx - 1);
+  const float fx = clamp01f(__fsub_rn(sx, (float)r.ic));
+  const float sy = __fmul_rn(y, a.inv_ds);
+  r.jc = cfloorf(sy, 0, a.ncy - 1);
+  const float fy = clamp01f(__fsub_rn(sy, (float)r.jc));
+  const long long FX = __float2int_rn(__fmul_rn(fx, 65536.0f));
+  const long long FY = __float2int_rn(__fmul_rn(fy, 65536.0f));
+  const long long GX = 65536 - FX, GY = 65536 - FY;
+  r.w00 = GX * GY;
+  r.w10 = FX * GY;
+  r.w01 = GX * FY;
+  r.w11 = FX * FY;
+  return r;
+}
+
+__device__ __forceinline__ bool finite4(const float4 &p) {
+  return isfinite(p.x) && isfinite(p.y) && isfinite(p.z) && isfinite(p.w);
+}
+
+}  // namespace cupic

@@ -1,0 +1,241 @@
+// jacobi.cu -- Poisson solve (5-point Jacobi, periodic in x, Dirichlet in y)
+// with the field derivation fused into the end of the last sweep
+// (reference: jacobi_iteration mesh.cu:297-381, its host loop
+// mesh.cu:55-120, field_derivation mesh.cu:385-472).
+//
+// The potential stays resident in shared memory for the whole solve: CTA c
+// of a cooperative grid of G CTAs owns interior node rows [r0, r1) and keeps
+// them, one halo row on each side, in two shared buffers (true Jacobi, not
+// the reference's in-place update, defect D5).  After every sweep each CTA
+// publishes its first and last row to an L2-resident exchange buffer and
+// raises a per-CTA sweep counter; a CTA waits only for its two neighbours.
+// Convergence checks use a grid barrier, and every wait is bounded: when a
+// wait gives up the kernel raises CUPIC_FLAG_TIMEOUT and all CTAs return.
+#include <math.h>
+
+#include "cupic_internal.cuh"
+#include "kernels.h"
+
+namespace cupic {
+
+namespace {
+
+constexpr int kJBlock = 1024;
+constexpr long long kSpinLimit = 1ll << 22;
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// spin until *p >= v; false if the wait gave up or another CTA aborted
+__device__ bool wait_geq(const unsigned *p, unsigned v, Ctl *ctl) {
+  for (long long it = 0; it < kSpinLimit; ++it) {
+    if (ld_acquire(p) >= v) return true;
+    if ((it & 255) == 255 && *(volatile int *)&ctl->abort) return false;
+    if (it > 32) __nanosleep(64);
+  }
+  atomicExch(&ctl->abort, 1);
+  atomicOr(&ctl->step_flags, (uint32_t)CUPIC_FLAG_TIMEOUT);
+  return false;
+}
+
+__device__ __forceinline__ float block_max(float v, float *red) {
+  v = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(v)));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    float w = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0f;
+    w = __uint_as_float(__reduce_max_sync(0xffffffffu, __float_as_uint(w)));
+    if (lane == 0) red[32] = w;
+  }
+  __syncthreads();
+  return red[32];
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kJBlock) k_jacobi(SimArgs a, JacobiArgs J) {
+  extern __shared__ float jsm[];
+  __shared__ float red[33];
+  __shared__ int bail;
+  const int c = blockIdx.x, G = J.G, tid = threadIdx.x;
+  const int nnx = a.nnx, P = J.pitch, Bm = J.rows_per_cta;
+  const int r0 = 1 + c * Bm;
+  const int r1 = min(r0 + Bm, a.nny - 1);
+  const int B = r1 - r0;
+  float *buf[2] = {jsm, jsm + (size_t)(Bm + 2) * P};
+  float *bsrc = jsm + (size_t)2 * (Bm + 2) * P;
+  Ctl *ctl = a.ctl;
+  if (tid == 0) bail = 0;
+
+  // phi rows r0-1 .. r1 into both buffers; source term of the owned rows
+  for (int k = tid; k < (B + 2) * nnx; k += kJBlock) {
+    const int lr = k / nnx, i = k - lr * nnx;
+    const float v = a.phi[(size_t)(r0 - 1 + lr) * nnx + i];
+    buf[0][lr * P + i] = v;
+    buf[1][lr * P + i] = v;
+  }
+  const long long *acc = reinterpret_cast<const long long *>(a.rho[ctl->cur]);
+  for (int k = tid; k < B * nnx; k += kJBlock) {
+    const int lr = k / nnx, i = k - lr * nnx;
+    const size_t rb = (size_t)(r0 + lr) * nnx;
+    const long long f = (i == 0 || i == nnx - 1) ? acc[rb] + acc[rb + nnx - 1] : acc[rb + i];
+    bsrc[lr * P + i] = __double2float_rn((double)f * a.cb);
+  }
+  __syncthreads();
+
+  const int W = nnx - 1;  // computed columns 0 .. nnx-2; column nnx-1 mirrors 0
+  int src = 0, done = 0, nchk = 0;
+  float last = INFINITY;
+  for (int s = 1; s <= J.max_sweeps; ++s) {
+    const float *S = buf[src];
+    float *D = buf[src ^ 1];
+    const bool check = (s % J.check_every == 0) || (s == J.max_sweeps);
+    float md = 0.0f;
+    for (int k = tid; k < B * W; k += kJBlock) {
+      const int lr = k / W + 1, i = k - (lr - 1) * W;
+      const float *cr = S + lr * P;
+      const float wv = (i == 0) ? cr[W - 1] : cr[i - 1];
+      const float v = __fmul_rn(
+          0.25f,
+          __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(bsrc[(lr - 1) * P + i], wv), cr[i + 1]), cr[P + i]),
+                    cr[i - P]));
+      D[lr * P + i] = v;
+      if (check) md = fmaxf(md, fabsf(__fsub_rn(v, cr[i])));
+      if (i == 0) {
+        D[lr * P + W] = v;
+        if (check) md = fmaxf(md, fabsf(__fsub_rn(v, cr[W])));
+      }
+    }
+    __syncthreads();
+    if (G > 1) {
+      float *hp = J.halo + ((size_t)(s & 1) * G + c) * 2 * P;
+      for (int i = tid; i < nnx; i += kJBlock) {
+        __stcg(hp + i, D[P + i]);
+        __stcg(hp + P + i, D[B * P + i]);
+      }
+      __syncthreads();
+      if (tid == 0) {
+        __threadfence();
+        st_release(&J.flags[c], (unsigned)s);
+        bool ok = true;
+        if (c > 0) ok = wait_geq(&J.flags[c - 1], (unsigned)s, ctl);
+        if (ok && c < G - 1) ok = wait_geq(&J.flags[c + 1], (unsigned)s, ctl);
+        if (!ok) bail = 1;
+      }
+      __syncthreads();
+      if (bail) break;
+      if (c > 0) {
+        const float *hn = J.halo + ((size_t)(s & 1) * G + (c - 1)) * 2 * P + P;
+        for (int i = tid; i < nnx; i += kJBlock) D[i] = __ldcg(hn + i);
+      }
+      if (c < G - 1) {
+        const float *hn = J.halo + ((size_t)(s & 1) * G + (c + 1)) * 2 * P;
+        for (int i = tid; i < nnx; i += kJBlock) D[(B + 1) * P + i] = __ldcg(hn + i);
+      }
+      __syncthreads();
+    }
+    src ^= 1;
+    done = s;
+    if (check) {
+      float bm = block_max(md, red);
+      if (G > 1) {
+        if (tid == 0) {
+          __stcg(&J.res_cta[(nchk & 1) * G + c], bm);
+          __threadfence();
+          atomicAdd(J.bar, 1u);
+          if (!wait_geq(J.bar, (unsigned)(G * (nchk + 1)), ctl)) bail = 1;
+        }
+        __syncthreads();
+        if (bail) break;
+        float v = 0.0f;
+        for (int k = tid; k < G; k += kJBlock) v = fmaxf(v, __ldcg(&J.res_cta[(nchk & 1) * G + k]));
+        bm = block_max(v, red);
+      }
+      ++nchk;
+      last = bm;
+      if (s >= J.min_sweeps && (double)bm < J.tol) break;
+    }
+  }
+
+  // write back the owned rows; derive E = -grad phi (mesh.cu:413-468)
+  const float *F = buf[src];
+  for (int k = tid; k < B * nnx; k += kJBlock) {
+    const int lr = k / nnx + 1, i = k - (lr - 1) * nnx;
+    a.phi[(size_t)(r0 + lr - 1) * nnx + i] = F[lr * P + i];
+  }
+  if (J.do_field) {
+    for (int k = tid; k < B * nnx; k += kJBlock) {
+      const int lr = k / nnx + 1, i = k - (lr - 1) * nnx;
+      const float *cr = F + lr * P;
+      const bool seam = (i == 0 || i == nnx - 1);
+      const float wv = seam ? cr[nnx - 2] : cr[i - 1];
+      const float ev = seam ? cr[1] : cr[i + 1];
+      float2 e;
+      e.x = __fdiv_rn(__fsub_rn(wv, ev), a.two_ds);
+      e.y = __fdiv_rn(__fsub_rn(cr[i - P], cr[i + P]), a.two_ds);
+      a.E[(size_t)(r0 + lr - 1) * nnx + i] = e;
+    }
+    if (c == 0) {
+      for (int i = tid; i < nnx; i += kJBlock)
+        a.E[i] = make_float2(0.0f, __fdiv_rn(__fsub_rn(F[i], F[P + i]), a.ds));
+    }
+    if (c == G - 1) {
+      for (int i = tid; i < nnx; i += kJBlock)
+        a.E[(size_t)(a.nny - 1) * nnx + i] =
+            make_float2(0.0f, __fdiv_rn(__fsub_rn(F[B * P + i], F[(B + 1) * P + i]), a.ds));
+    }
+  }
+  if (J.write_stats && c == 0 && tid == 0) {
+    ctl->sweeps = done;
+    ctl->residual = last;
+  }
+}
+
+size_t jacobi_smem_bytes(int rows_per_cta, int pitch) {
+  return (size_t)(3 * rows_per_cta + 4) * pitch * sizeof(float);
+}
+
+int jacobi_block() { return kJBlock; }
+
+// the attribute only grows, so contexts of different sizes can coexist
+cudaError_t jacobi_set_smem(size_t bytes) {
+  static size_t cur = 0;
+  if (bytes <= cur) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
+
+cudaError_t jacobi_max_ctas(size_t smem, int *per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_jacobi, kJBlock, smem);
+}
+
+cudaError_t launch_jacobi(const SimArgs &a, const JacobiArgs &J, cudaStream_t st) {
+  const size_t sm = jacobi_smem_bytes(J.rows_per_cta, J.pitch);
+  if (J.G > 1) {
+    cudaError_t e = cudaMemsetAsync(J.flags, 0, sizeof(unsigned) * (J.G + 1), st);
+    if (e != cudaSuccess) return e;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(J.G);
+  cfg.blockDim = dim3(kJBlock);
+  cfg.dynamicSmemBytes = sm;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_jacobi, a, J);
+}
+
+}  // namespace cupic

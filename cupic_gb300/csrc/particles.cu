@@ -1,0 +1,534 @@
+// particles.cu -- particle kernels of the GB300 PIC cycle.
+//
+// Storage: per species, y cell row j owns the segment
+// parts[seg[j] .. seg[j]+cap[j]) of float4 {x,y,vx,vy}; its live particles
+// are the prefix of length cnt[j].  One step's particle work is
+//   k_push_deposit  gather + leapfrog + wrap + classify; stable in-place
+//                   compaction of the row's stayers, staging of the movers
+//                   to the neighbouring rows, and deposition of every moved
+//                   particle into the next charge accumulator (fused; the
+//                   reference runs fast_grid_to_particle, leap_frog_step,
+//                   pDefragDown/Up, pRebracketing, bmHandler, pCyclicCC and
+//                   fast_particle_to_grid as separate passes)
+//   k_arrive        appends the movers from the rows below and above
+//   k_inject        draws the injected flux of the step (cc.cu:179-256),
+//                   appends it to the rows it falls in, deposits it
+//   k_finalize      per-step counters, clock advance, charge buffer flip
+#include "cupic_internal.cuh"
+#include "kernels.h"
+
+namespace cupic {
+
+namespace {
+
+constexpr int kPushBlock = 512;
+constexpr int kPushPPT = 2;
+constexpr int kInjBlock = 1024;
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ void raise_flags(Ctl *ctl, uint32_t f) {
+  if (f) atomicOr(&ctl->step_flags, f);
+}
+
+// shared tile of node rows [row0, row0+nrows) of the charge accumulator;
+// deposits that fall outside go straight to global memory
+struct RhoTile {
+  unsigned long long *t;
+  int row0, nrows, nnx;
+  unsigned long long *g;
+
+  __device__ __forceinline__ void add(int node_row, int i, long long v) const {
+    const int tr = node_row - row0;
+    if (tr >= 0 && tr < nrows) {
+      atomicAdd(&t[tr * nnx + i], (unsigned long long)v);
+    } else {
+      atomicAdd(&g[(size_t)node_row * nnx + i], (unsigned long long)v);
+    }
+  }
+  __device__ __forceinline__ void deposit(const SimArgs &a, float x, float y, long long q) const {
+    const CicFixed c = cic_fixed(a, x, y);
+    add(c.jc, c.ic, q * c.w00);
+    add(c.jc, c.ic + 1, q * c.w10);
+    add(c.jc + 1, c.ic, q * c.w01);
+    add(c.jc + 1, c.ic + 1, q * c.w11);
+  }
+};
+
+__device__ __forceinline__ void flush_tile(const RhoTile &T, int nny) {
+  for (int k = threadIdx.x; k < T.nrows * T.nnx; k += blockDim.x) {
+    const int r = T.row0 + k / T.nnx;
+    const unsigned long long v = T.t[k];
+    if (v != 0ull && r >= 0 && r < nny) atomicAdd(&T.g[(size_t)r * T.nnx + (k % T.nnx)], v);
+  }
+}
+
+// classification of a pushed particle listed in row s (s < 0: injected)
+struct Cls {
+  int dest;  // row, kRowAbsorbed or kRowRemoved
+  uint32_t flag;
+};
+
+__device__ __forceinline__ Cls classify(const SimArgs &a, const float4 &p, int s) {
+  if (!finite4(p)) return {kRowRemoved, CUPIC_FLAG_NONFINITE};
+  if (p.y < 0.0f) return {kRowAbsorbed, 0u};
+  if (p.y >= a.Ly) return {kRowRemoved, 0u};
+  uint32_t f = 0;
+  if (p.x < 0.0f || p.x >= a.Lx) f |= CUPIC_FLAG_XRANGE;
+  const int d = row_of(a, p.y);
+  if (s >= 0 && (d > s + 1 || d < s - 1)) return {s, f | CUPIC_FLAG_CFL};
+  return {d, f};
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// initial plasma (init.cu:159-179, with the project's counter-based draws)
+// ---------------------------------------------------------------------------
+__global__ void k_init_particles(SimArgs a) {
+  const int j = blockIdx.x, sp = blockIdx.y;
+  const SpeciesDev &S = a.sp[sp];
+  float4 *row = S.parts + S.seg[j];
+  const double sig = a.sig[sp];
+  for (int k = threadIdx.x; k < a.ppr; k += blockDim.x) {
+    const uint4 r = philox4x32_10(
+        make_uint4((uint32_t)k, (uint32_t)j, 0u, (uint32_t)((kPurposeInit << 8) | sp)), a.k0, a.k1);
+    const double x = u01(r.x) * a.Lx_d;
+    const double y = ((double)j + u01(r.y)) * a.ds_d;
+    const double rr = sqrt(-2.0 * dev_log(u01(r.z)));
+    double sn, cs;
+    dev_sincos2pi(u01(r.w), &sn, &cs);
+    float4 p = make_float4((float)x, (float)y, (float)(sig * (rr * cs)), (float)(sig * (rr * sn)));
+    p.x = wrap_x(a, p.x);
+    for (int it = 0; it < 16 && row_of(a, p.y) > j; ++it) p.y = nextafterf(p.y, 0.0f);
+    for (int it = 0; it < 16 && row_of(a, p.y) < j; ++it) p.y = nextafterf(p.y, a.Ly);
+    row[k] = p;
+  }
+  if (threadIdx.x == 0) S.cnt[j] = a.ppr;
+}
+
+// ---------------------------------------------------------------------------
+// charge deposition of the current particles into rho[ctl->cur]
+// (mesh.cu:162-293; int64 fixed point, so the sum is order independent)
+// ---------------------------------------------------------------------------
+__global__ void k_deposit(SimArgs a) {
+  extern __shared__ unsigned long long dtile[];
+  const int s = blockIdx.x;
+  RhoTile T{dtile, s, 2, a.nnx, a.rho[a.ctl->cur]};
+  for (int k = threadIdx.x; k < 2 * a.nnx; k += blockDim.x) dtile[k] = 0ull;
+  __syncthreads();
+  for (int sp = 0; sp < 2; ++sp) {
+    const SpeciesDev &S = a.sp[sp];
+    const float4 *row = S.parts + S.seg[s];
+    const int n = S.cnt[s];
+    const long long q = sp == 0 ? -1 : 1;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      const float4 p = row[k];
+      T.deposit(a, p.x, p.y, q);
+    }
+  }
+  __syncthreads();
+  flush_tile(T, a.nny);
+}
+
+// zero the accumulator the next deposit writes (rho[cur^1])
+__global__ void k_zero_next_rho(SimArgs a) {
+  unsigned long long *r = a.rho[a.ctl->cur ^ 1];
+  const size_t n = (size_t)a.nnx * a.nny;
+  for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
+       k += (size_t)gridDim.x * blockDim.x)
+    r[k] = 0ull;
+}
+
+// ---------------------------------------------------------------------------
+// leapfrog start: v -= dt/2 q E / m (init.cu:264-323, 793-833)
+// ---------------------------------------------------------------------------
+__global__ void k_leapfrog_start(SimArgs a) {
+  extern __shared__ float2 etile[];
+  const int s = blockIdx.x;
+  for (int k = threadIdx.x; k < 2 * a.nnx; k += blockDim.x) etile[k] = a.E[(size_t)s * a.nnx + k];
+  __syncthreads();
+  for (int sp = 0; sp < 2; ++sp) {
+    const SpeciesDev &S = a.sp[sp];
+    float4 *row = S.parts + S.seg[s];
+    const int n = S.cnt[s];
+    const float h = a.mhdtqm[sp];
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      float4 p = row[k];
+      float ex, ey;
+      gather_tile(a, etile, p.x, p.y, s, ex, ey);
+      p.z = __fmaf_rn(h, ex, p.z);
+      p.w = __fmaf_rn(h, ey, p.w);
+      row[k] = p;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// fused push + wrap + row binning + deposition, one block per cell row s
+// handling both species (particles.cu:110-231, cc.cu:303-810, mesh.cu:162-293)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kPushBlock) k_push_deposit(SimArgs a) {
+  extern __shared__ unsigned long long psm[];
+  constexpr int NW = kPushBlock / 32;
+  const int s = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nnx = a.nnx;
+  unsigned long long *rtile = psm;                       // 4 node rows s-1..s+2
+  float2 *etile = reinterpret_cast<float2 *>(psm + 4 * nnx);  // node rows s, s+1
+  __shared__ uint32_t wsum[NW];
+  __shared__ uint32_t woff[NW];
+  __shared__ uint32_t wtot;
+  __shared__ unsigned long long s_abs, s_rem;
+
+  Ctl *ctl = a.ctl;
+  RhoTile T{rtile, s - 1, 4, nnx, a.rho[ctl->cur ^ 1]};
+  for (int k = tid; k < 4 * nnx; k += kPushBlock) rtile[k] = 0ull;
+  for (int k = tid; k < 2 * nnx; k += kPushBlock) etile[k] = a.E[(size_t)s * nnx + k];
+  __syncthreads();
+
+  uint32_t fl = 0;
+  const uint32_t lt = (1u << lane) - 1u;
+  for (int sp = 0; sp < 2; ++sp) {
+    const SpeciesDev &S = a.sp[sp];
+    const int n = S.cnt[s];
+    float4 *row = S.parts + S.seg[s];
+    float4 *sup = S.stage_up + (size_t)s * S.stage_cap;
+    float4 *sdn = S.stage_down + (size_t)s * S.stage_cap;
+    const float dtqm = a.dtqm[sp];
+    const long long q = sp == 0 ? -1 : 1;
+    int c_stay = 0, c_up = 0, c_dn = 0;
+    unsigned nabs = 0, nrem = 0;
+    if (tid == 0) {
+      s_abs = 0ull;
+      s_rem = 0ull;
+    }
+    for (int base = 0; base < n; base += kPushBlock * kPushPPT) {
+      float4 pv[kPushPPT];
+#pragma unroll
+      for (int j = 0; j < kPushPPT; ++j) {
+        const int idx = base + j * kPushBlock + tid;
+        if (idx < n) pv[j] = row[idx];
+      }
+#pragma unroll
+      for (int j = 0; j < kPushPPT; ++j) {
+        const int idx = base + j * kPushBlock + tid;
+        const bool valid = idx < n;
+        float4 p = pv[j];
+        int cat = 3;  // 0 stay, 1 up, 2 down, 3 none
+        if (valid) {
+          float ex, ey;
+          gather_tile(a, etile, p.x, p.y, s, ex, ey);
+          p.z = __fmaf_rn(dtqm, ex, p.z);
+          p.w = __fmaf_rn(dtqm, ey, p.w);
+          p.x = __fmaf_rn(a.dt, p.z, p.x);
+          p.y = __fmaf_rn(a.dt, p.w, p.y);
+          p.x = wrap_x(a, p.x);
+          const Cls c = classify(a, p, s);
+          fl |= c.flag;
+          if (c.dest == kRowAbsorbed) {
+            ++nabs;
+          } else if (c.dest == kRowRemoved) {
+            ++nrem;
+          } else {
+            cat = c.dest == s ? 0 : (c.dest == s + 1 ? 1 : 2);
+          }
+        }
+        const uint32_t bs = __ballot_sync(kFull, cat == 0);
+        const uint32_t bu = __ballot_sync(kFull, cat == 1);
+        const uint32_t bd = __ballot_sync(kFull, cat == 2);
+        if (lane == 0) wsum[warp] = __popc(bs) | (__popc(bu) << 10) | (__popc(bd) << 20);
+        __syncthreads();
+        if (warp == 0) {
+          const uint32_t v = lane < NW ? wsum[lane] : 0u;
+          uint32_t inc = v;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t u = __shfl_up_sync(kFull, inc, o);
+            if (lane >= o) inc += u;
+          }
+          if (lane < NW) woff[lane] = inc - v;
+          if (lane == 31) wtot = inc;
+        }
+        __syncthreads();
+        const uint32_t off = woff[warp], tot = wtot;
+        if (cat == 0) {
+          const int pos = c_stay + (int)(off & 1023u) + __popc(bs & lt);
+          row[pos] = p;
+        } else if (cat == 1) {
+          const int pos = c_up + (int)((off >> 10) & 1023u) + __popc(bu & lt);
+          if (pos < S.stage_cap) sup[pos] = p; else fl |= CUPIC_FLAG_STAGE;
+        } else if (cat == 2) {
+          const int pos = c_dn + (int)((off >> 20) & 1023u) + __popc(bd & lt);
+          if (pos < S.stage_cap) sdn[pos] = p; else fl |= CUPIC_FLAG_STAGE;
+        }
+        if (cat < 3) T.deposit(a, p.x, p.y, q);
+        c_stay += (int)(tot & 1023u);
+        c_up += (int)((tot >> 10) & 1023u);
+        c_dn += (int)((tot >> 20) & 1023u);
+        __syncthreads();
+      }
+    }
+    const unsigned wa = __reduce_add_sync(kFull, nabs), wr = __reduce_add_sync(kFull, nrem);
+    if (lane == 0 && (wa | wr)) {
+      atomicAdd(&s_abs, (unsigned long long)wa);
+      atomicAdd(&s_rem, (unsigned long long)wr);
+    }
+    __syncthreads();
+    if (tid == 0) {
+      S.nstay[s] = c_stay;
+      S.nup[s] = min(c_up, S.stage_cap);
+      S.ndown[s] = min(c_dn, S.stage_cap);
+      if (s_abs) atomicAdd(&ctl->absorbed[sp], s_abs);
+      if (s_rem) atomicAdd(&ctl->removed[sp], s_rem);
+    }
+    __syncthreads();
+  }
+  flush_tile(T, a.nny);
+  fl = __reduce_or_sync(kFull, fl);
+  if (lane == 0) raise_flags(ctl, fl);
+}
+
+// ---------------------------------------------------------------------------
+// append the movers: row d = [stayed] + [up from d-1] + [down from d+1]
+// ---------------------------------------------------------------------------
+__global__ void k_arrive(SimArgs a) {
+  const int d = blockIdx.x, sp = blockIdx.y;
+  const SpeciesDev &S = a.sp[sp];
+  const int ns = S.nstay[d];
+  const int nb = d > 0 ? S.nup[d - 1] : 0;
+  const int na = d + 1 < a.ncy ? S.ndown[d + 1] : 0;
+  const int capd = S.cap[d];
+  float4 *row = S.parts + S.seg[d];
+  if (nb) {
+    const float4 *src = S.stage_up + (size_t)(d - 1) * S.stage_cap;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x)
+      if (ns + k < capd) row[ns + k] = src[k];
+  }
+  if (na) {
+    const float4 *src = S.stage_down + (size_t)(d + 1) * S.stage_cap;
+    for (int k = threadIdx.x; k < na; k += blockDim.x)
+      if (ns + nb + k < capd) row[ns + nb + k] = src[k];
+  }
+  if (threadIdx.x == 0) {
+    const int tot = ns + nb + na;
+    if (tot > capd) raise_flags(a.ctl, CUPIC_FLAG_CAPACITY);
+    S.cnt[d] = min(tot, capd);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// injection of the half-Maxwellian flux at y = Ly (cc.cu:179-256), one block
+// per species.  Draw k of step i uses Philox counter {k, i_lo, i_hi, 1<<8|sp}.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kInjBlock) k_inject(SimArgs a) {
+  extern __shared__ int running[];  // [ncy] injected per destination row
+  constexpr int NW = kInjBlock / 32;
+  const int sp = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const SpeciesDev &S = a.sp[sp];
+  Ctl *ctl = a.ctl;
+  __shared__ int s_in;
+  __shared__ double s_t;
+  __shared__ unsigned s_rem;
+  if (tid == 0) {
+    const double t = ctl->t;
+    const double fpt = t + a.dt_d;
+    if (!ctl->tin_set[sp]) {
+      ctl->tin[sp] = t + a.dtin[sp];
+      ctl->tin_set[sp] = 1;
+    }
+    double tin = ctl->tin[sp];
+    int in = 0;
+    if (tin < fpt) in = 1 + (int)((fpt - tin) / a.dtin[sp]);
+    const int ne = in < S.inj_cap ? in : S.inj_cap;
+    if (in > ne) atomicOr(&ctl->step_flags, (uint32_t)CUPIC_FLAG_CAPACITY);
+    for (int k = 0; k < in; ++k) {
+      if (k < ne) S.inj_tin[k] = tin;
+      tin += a.dtin[sp];
+    }
+    ctl->tin[sp] = tin;
+    ctl->inj_count[sp] = in;
+    s_in = ne;
+    s_t = t;
+    s_rem = 0;
+  }
+  for (int k = tid; k < a.ncy; k += kInjBlock) running[k] = 0;
+  __syncthreads();
+  const int ne = s_in;
+  const double t = s_t, fpt = t + a.dt_d, fvt = t + 0.5 * a.dt_d;
+  const double sig = a.sig[sp], qm = a.qm[sp];
+  const long long q = sp == 0 ? -1 : 1;
+  const int64_t step = ctl->step;
+  const size_t top = (size_t)(a.nny - 1) * a.nnx;
+  unsigned long long *rho_next = a.rho[ctl->cur ^ 1];
+  uint32_t fl = 0;
+  unsigned nrem = 0;
+  for (int base = 0; base < ne; base += kInjBlock) {
+    const int k = base + tid;
+    int d = kRowRemoved;
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (k < ne) {
+      const uint4 r = philox4x32_10(
+          make_uint4((uint32_t)k, (uint32_t)step, (uint32_t)((uint64_t)step >> 32),
+                     (uint32_t)((kPurposeInject << 8) | sp)),
+          a.k0, a.k1);
+      double x = u01(r.x) * a.Lx_d;
+      double sn, cs;
+      dev_sincos2pi(u01(r.z), &sn, &cs);
+      double vx = sig * (sqrt(-2.0 * dev_log(u01(r.y))) * cs);
+      double vy = -(sig * sqrt(-2.0 * dev_log(u01(r.w))));
+      const int ic = cfloord(x * a.inv_ds_d, 0, a.ncx - 1);
+      const double fx = clamp01d(x * a.inv_ds_d - (double)ic);
+      const float2 e0 = a.E[top + ic], e1 = a.E[top + ic + 1];
+      const double epx = (1.0 - fx) * (double)e0.x + fx * (double)e1.x;
+      const double epy = (1.0 - fx) * (double)e0.y + fx * (double)e1.y;
+      const double tin = S.inj_tin[k];
+      const double dp = fpt - tin, dv = fvt - tin;
+      x = x + dp * vx;
+      const double y = a.Ly_d + dp * vy;
+      vx = vx + dv * (qm * epx);
+      vy = vy + dv * (qm * epy);
+      p = make_float4((float)x, (float)y, (float)vx, (float)vy);
+      p.x = wrap_x(a, p.x);
+      const Cls c = classify(a, p, -1);
+      fl |= c.flag;
+      d = c.dest;
+      if (d < 0) ++nrem;
+    }
+    // stable rank of each draw within its destination row, in draw order
+    const int key = d >= 0 ? d : -1 - lane;
+    const uint32_t grp = __match_any_sync(kFull, key);
+    const int leader = __ffs(grp) - 1;
+    const int rank = __popc(grp & ((1u << lane) - 1u));
+    int basev = 0;
+    for (int w = 0; w < NW; ++w) {
+      if (warp == w && d >= 0 && lane == leader) {
+        basev = running[d];
+        running[d] = basev + __popc(grp);
+      }
+      __syncthreads();
+    }
+    const int b0 = __shfl_sync(kFull, basev, leader);
+    if (d >= 0) {
+      const int pos = S.cnt[d] + b0 + rank;
+      if (pos < S.cap[d]) {
+        S.parts[S.seg[d] + pos] = p;
+        const CicFixed c = cic_fixed(a, p.x, p.y);
+        atomicAdd(&rho_next[(size_t)c.jc * a.nnx + c.ic], (unsigned long long)(q * c.w00));
+        atomicAdd(&rho_next[(size_t)c.jc * a.nnx + c.ic + 1], (unsigned long long)(q * c.w10));
+        atomicAdd(&rho_next[(size_t)(c.jc + 1) * a.nnx + c.ic], (unsigned long long)(q * c.w01));
+        atomicAdd(&rho_next[(size_t)(c.jc + 1) * a.nnx + c.ic + 1],
+                  (unsigned long long)(q * c.w11));
+      } else {
+        fl |= CUPIC_FLAG_CAPACITY;
+      }
+    }
+  }
+  const unsigned wr = __reduce_add_sync(kFull, nrem);
+  if (lane == 0 && wr) atomicAdd(&s_rem, wr);
+  fl = __reduce_or_sync(kFull, fl);
+  if (lane == 0) raise_flags(ctl, fl);
+  __syncthreads();
+  for (int k = tid; k < a.ncy; k += kInjBlock)
+    if (running[k]) S.cnt[k] = min(S.cnt[k] + running[k], S.cap[k]);
+  if (tid == 0 && s_rem) atomicAdd(&ctl->removed[sp], (unsigned long long)s_rem);
+}
+
+// ---------------------------------------------------------------------------
+// end of step: stats ring entry, clocks, charge buffer flip
+// ---------------------------------------------------------------------------
+__global__ void k_finalize(SimArgs a) {
+  Ctl *ctl = a.ctl;
+  __shared__ unsigned long long live[2];
+  if (threadIdx.x < 2) live[threadIdx.x] = 0ull;
+  __syncthreads();
+  for (int sp = 0; sp < 2; ++sp) {
+    unsigned long long v = 0;
+    for (int k = threadIdx.x; k < a.ncy; k += blockDim.x) v += (unsigned long long)a.sp[sp].cnt[k];
+    atomicAdd(&live[sp], v);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    cupic_step_stats &st = ctl->ring[ctl->step % kStatsRing];
+    st.step = ctl->step;
+    st.t = ctl->t;
+    for (int sp = 0; sp < 2; ++sp) {
+      st.absorbed[sp] = (int64_t)ctl->absorbed[sp];
+      st.removed[sp] = (int64_t)ctl->removed[sp];
+      st.injected[sp] = ctl->inj_count[sp];
+      st.live[sp] = (int64_t)live[sp];
+      ctl->absorbed[sp] = 0ull;
+      ctl->removed[sp] = 0ull;
+      ctl->inj_count[sp] = 0;
+    }
+    st.sweeps = ctl->sweeps;
+    st.residual = ctl->residual;
+    st.flags = ctl->step_flags;
+    ctl->flags |= ctl->step_flags;
+    ctl->step_flags = 0u;
+    ctl->t = ctl->t + a.dt_d;
+    ctl->step = ctl->step + 1;
+    ctl->cur ^= 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// launch helpers
+// ---------------------------------------------------------------------------
+cudaError_t launch_init_particles(const SimArgs &a, cudaStream_t st) {
+  k_init_particles<<<dim3(a.ncy, 2), 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_deposit(const SimArgs &a, cudaStream_t st) {
+  k_deposit<<<a.ncy, 256, 2 * a.nnx * sizeof(unsigned long long), st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_zero_next_rho(const SimArgs &a, cudaStream_t st) {
+  const size_t n = (size_t)a.nnx * a.nny;
+  int blocks = (int)((n + 1023) / 1024);
+  if (blocks > 1184) blocks = 1184;
+  k_zero_next_rho<<<blocks, 1024, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_leapfrog_start(const SimArgs &a, cudaStream_t st) {
+  k_leapfrog_start<<<a.ncy, 256, 2 * a.nnx * sizeof(float2), st>>>(a);
+  return cudaGetLastError();
+}
+
+size_t push_smem_bytes(int nnx) {
+  return (size_t)4 * nnx * sizeof(unsigned long long) + (size_t)2 * nnx * sizeof(float2);
+}
+
+// the attribute only grows, so contexts of different sizes can coexist
+cudaError_t push_set_smem(size_t bytes) {
+  static size_t cur = 48 * 1024;
+  if (bytes <= cur) return cudaSuccess;
+  cudaError_t e =
+      cudaFuncSetAttribute(k_push_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
+
+cudaError_t launch_push_deposit(const SimArgs &a, cudaStream_t st) {
+  const size_t sm = push_smem_bytes(a.nnx);
+  k_push_deposit<<<a.ncy, kPushBlock, sm, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_arrive(const SimArgs &a, cudaStream_t st) {
+  k_arrive<<<dim3(a.ncy, 2), 128, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_inject(const SimArgs &a, cudaStream_t st) {
+  k_inject<<<2, kInjBlock, a.ncy * sizeof(int), st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize(const SimArgs &a, cudaStream_t st) {
+  k_finalize<<<1, 256, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+}  // namespace cupic

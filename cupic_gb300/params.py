@@ -1,0 +1,116 @@
+"""ctypes mirror of ``cupic_params`` / ``cupic_step_stats`` (include/cupic_gpu.h).
+
+The fields are the reference's normalised input_data parameters
+(src/init.cu:451-789 of AntonioTejero/cupic) plus the Jacobi stop rule and
+storage knobs of this build.  ``workload_params`` builds the parameter sets
+of the named workloads directly in normalised units.
+"""
+import ctypes
+
+_PARAM_FIELDS = [
+    ("ncx", ctypes.c_int32), ("ncy", ctypes.c_int32),
+    ("ds", ctypes.c_double), ("dt", ctypes.c_double),
+    ("n", ctypes.c_double), ("eps0", ctypes.c_double), ("phi_p", ctypes.c_double),
+    ("me", ctypes.c_double), ("mi", ctypes.c_double),
+    ("kte", ctypes.c_double), ("kti", ctypes.c_double),
+    ("qe", ctypes.c_double), ("qi", ctypes.c_double),
+    ("tol", ctypes.c_double),
+    ("min_sweeps", ctypes.c_int32), ("max_sweeps", ctypes.c_int32), ("check_every", ctypes.c_int32),
+    ("init_tol", ctypes.c_double),
+    ("init_min_sweeps", ctypes.c_int32), ("init_max_sweeps", ctypes.c_int32),
+    ("n_ini", ctypes.c_int32), ("n_prev", ctypes.c_int32), ("n_save", ctypes.c_int32),
+    ("n_fin", ctypes.c_int32),
+    ("ppr", ctypes.c_int32),
+    ("row_slack", ctypes.c_double), ("stage_frac", ctypes.c_double),
+    ("seed", ctypes.c_uint64),
+]
+
+
+class Params(ctypes.Structure):
+    _fields_ = _PARAM_FIELDS
+
+    def finalize(self):
+        """ppr = int(n*Lx*ds*ds), the initial particles per row (init.cu:136)."""
+        lx = self.ds * self.ncx
+        self.ppr = int(self.n * lx * self.ds * self.ds)
+        return self
+
+    def copy(self):
+        c = Params()
+        ctypes.pointer(c)[0] = self
+        return c
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in _PARAM_FIELDS}
+
+    @property
+    def nnx(self):
+        return self.ncx + 1
+
+    @property
+    def nny(self):
+        return self.ncy + 1
+
+
+class StepStats(ctypes.Structure):
+    _fields_ = [
+        ("step", ctypes.c_int64), ("t", ctypes.c_double),
+        ("absorbed", ctypes.c_int64 * 2), ("removed", ctypes.c_int64 * 2),
+        ("injected", ctypes.c_int64 * 2), ("live", ctypes.c_int64 * 2),
+        ("sweeps", ctypes.c_int32), ("residual", ctypes.c_float), ("flags", ctypes.c_uint32),
+    ]
+
+    def as_dict(self):
+        return {
+            "step": self.step, "t": self.t,
+            "absorbed": list(self.absorbed), "removed": list(self.removed),
+            "injected": list(self.injected), "live": list(self.live),
+            "sweeps": self.sweeps, "residual": self.residual, "flags": self.flags,
+        }
+
+
+def workload_params(name="small", **over):
+    """Parameter sets of the named workloads, in normalised units.
+
+    small : 64x256 cells, ds=0.5, 20 particles per cell per species
+            (n=160), mi/me=100, Ti/Te=1, phi_p=-5, dt=0.05, Jacobi to
+            max|dphi|<1e-6 with at most 2000 sweeps, seed 0.
+    large : 512x2048 cells, ds=0.5, 100 particles per cell per species
+            (n=800), mi/me=1836, Ti/Te=0.1, phi_p=-5, dt=0.05, 200 fixed
+            Jacobi sweeps, seed 1.
+    tiny  : 16x32 cells, 8 particles per cell, for quick tests.
+    """
+    p = Params()
+    p.ds, p.dt = 0.5, 0.05
+    p.me, p.kte, p.qe, p.qi = 1.0, 1.0, -1.0, 1.0
+    p.phi_p = -5.0
+    p.check_every = 1
+    p.init_tol, p.init_min_sweeps, p.init_max_sweeps = 1e-3, 1, 2000
+    p.n_ini, p.n_prev, p.n_save, p.n_fin = 0, 0, 100, 1000
+    p.row_slack, p.stage_frac = 0.5, 0.25
+    if name == "small":
+        p.ncx, p.ncy = 64, 256
+        p.n = 160.0
+        p.mi, p.kti = 100.0, 1.0
+        p.tol, p.min_sweeps, p.max_sweeps = 1e-6, 1, 2000
+        p.seed = 0
+    elif name == "large":
+        p.ncx, p.ncy = 512, 2048
+        p.n = 800.0
+        p.mi, p.kti = 1836.0, 0.1
+        p.tol, p.min_sweeps, p.max_sweeps = 0.0, 200, 200
+        p.init_tol, p.init_min_sweeps, p.init_max_sweeps = 0.0, 200, 200
+        p.seed = 1
+    elif name == "tiny":
+        p.ncx, p.ncy = 16, 32
+        p.n = 64.0
+        p.mi, p.kti = 100.0, 1.0
+        p.tol, p.min_sweeps, p.max_sweeps = 1e-6, 1, 400
+        p.init_max_sweeps = 400
+        p.seed = 7
+    else:
+        raise ValueError(f"unknown workload {name!r}")
+    p.eps0 = p.n
+    for k, v in over.items():
+        setattr(p, k, v)
+    return p.finalize()

@@ -1,0 +1,201 @@
+/*
+ * cupic_gpu.h -- C-ABI of the GB300 (sm_103a) electrostatic PIC cycle.
+ *
+ * One handle (cupic_ctx) owns the device state of one probe/plasma slab:
+ * particles of both species (FP32, float4 {x,y,vx,vy} per particle, grouped
+ * by y cell row), the potential phi (FP32), the field E (FP32 pairs) and the
+ * charge accumulator rho (int64 fixed point, 2^32 per unit macroparticle
+ * charge).  Every call returns an int status (CUPIC_OK == 0); nothing calls
+ * exit().  All pointers in this header are HOST pointers unless a name says
+ * otherwise; no torch or CUDA types appear in the signatures.
+ *
+ * The entry points replace the reference's host functions, which have C++
+ * linkage and global state (reference file:line given per function):
+ *   charge_deposition   src/mesh.cu:15-51        -> cupic_charge_deposition
+ *   poisson_solver      src/mesh.cu:55-120       -> cupic_poisson_solver
+ *   field_solver        src/mesh.cu:124-154      -> cupic_field_solver
+ *   particle_mover      src/particles.cu:15-102  -> cupic_particle_mover
+ *   cc                  src/cc.cu:15-69          -> cupic_cc
+ *   init_sim            src/init.cu:57-102       -> cupic_init_plasma
+ *   read_input_file +   src/init.cu:424-789      -> cupic_params_from_input_data
+ *     init_* getters
+ *   read_particle_file  src/init.cu:348-420      -> cupic_load_particles
+ *   particles_snapshot  src/diagnostic.cu:48-87  -> cupic_store_particles
+ *   mesh_snapshot       src/diagnostic.cu:91-133 -> cupic_get_rho / cupic_get_phi
+ *   number_of_particles src/diagnostic.cu:15-44  -> cupic_get_counts
+ */
+#ifndef CUPIC_GPU_H
+#define CUPIC_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  CUPIC_OK = 0,
+  CUPIC_ERR_ARG = 1,        /* invalid argument / parameter */
+  CUPIC_ERR_CUDA = 2,       /* a CUDA runtime call failed */
+  CUPIC_ERR_NOMEM = 3,      /* device or host allocation failed */
+  CUPIC_ERR_IO = 4,         /* input_data / particle file could not be read */
+  CUPIC_ERR_CAPACITY = 5,   /* a row or staging buffer would overflow */
+  CUPIC_ERR_CFL = 6,        /* a particle moved more than one cell row in a step */
+  CUPIC_ERR_NONFINITE = 7,  /* a NaN/Inf particle coordinate was seen */
+  CUPIC_ERR_STATE = 8,      /* call out of order (e.g. step before init) */
+  CUPIC_ERR_TIMEOUT = 9,    /* a bounded device-side wait gave up */
+  CUPIC_ERR_NODEVICE = 10   /* no CUDA device visible */
+};
+
+/* device-side flag bits, as returned by cupic_get_flags() */
+enum {
+  CUPIC_FLAG_CFL = 1u << 0,
+  CUPIC_FLAG_CAPACITY = 1u << 1,
+  CUPIC_FLAG_STAGE = 1u << 2,
+  CUPIC_FLAG_NONFINITE = 1u << 3,
+  CUPIC_FLAG_TIMEOUT = 1u << 4,
+  CUPIC_FLAG_XRANGE = 1u << 5
+};
+
+enum { CUPIC_ELECTRONS = 0, CUPIC_IONS = 1 };
+
+/*
+ * Normalised simulation parameters.  Units follow the reference
+ * (src/init.cu:451-789): lengths in Debye lengths, time in 1/omega_pe,
+ * masses in m_e, energies in kT_e, potential in kT_e/e, density in
+ * particles per Debye-length cube.
+ */
+typedef struct cupic_params {
+  int32_t ncx, ncy;         /* cells in x (periodic) and y (input_data lines 10, 11) */
+  double ds;                /* cell size (line 12) */
+  double dt;                /* time step (line 13) */
+  double n;                 /* density n = ne*lambda_D^3 (init.cu:542-556) */
+  double eps0;              /* permittivity (init.cu:612-630); equals n in exact arithmetic */
+  double phi_p;             /* probe potential at y=0 (init.cu:523-538) */
+  double me, mi;            /* masses (init.cu:473-494): 1, gamma */
+  double kte, kti;          /* thermal energies (init.cu:498-519): 1, beta */
+  double qe, qi;            /* charges (init.cu:451-469): -1, +1 */
+  /* Jacobi control for each step (main.cu:64; mesh.cu:94-114).  A sweep
+   * count s stops the solve when s >= min_sweeps and the max |delta phi| of
+   * a checked sweep is < tol, or when s == max_sweeps.  A sweep is checked
+   * when s % check_every == 0 or s == max_sweeps. */
+  double tol;
+  int32_t min_sweeps, max_sweeps, check_every;
+  /* the same for the initial solve (init.cu:254) */
+  double init_tol;
+  int32_t init_min_sweeps, init_max_sweeps;
+  /* run control copied from input_data lines 1-4 (main.cu:33-36) */
+  int32_t n_ini, n_prev, n_save, n_fin;
+  /* particles per y row per species at t=0: int(n*Lx*ds*ds) (init.cu:136) */
+  int32_t ppr;
+  /* storage: row capacity = ceil(ppr*(1+row_slack)) + 64; movers staged per
+   * row up to ceil(capacity*stage_frac) + 64 */
+  double row_slack;
+  double stage_frac;
+  /* seed of the counter-based generator (Philox4x32-10) used for the
+   * initial plasma and the injected flux */
+  uint64_t seed;
+} cupic_params;
+
+/* Per-step counters (absorbed = crossed y<0 into the probe; removed =
+ * crossed y>=Ly; injected = half-Maxwellian flux at y=Ly). */
+typedef struct cupic_step_stats {
+  int64_t step;             /* index i of the step in the main loop */
+  double t;                 /* time passed to the boundary stage */
+  int64_t absorbed[2];      /* [electrons, ions] */
+  int64_t removed[2];
+  int64_t injected[2];
+  int64_t live[2];          /* particles after the step */
+  int32_t sweeps;           /* Jacobi sweeps of the step */
+  float residual;           /* max |delta phi| of the last checked sweep */
+  uint32_t flags;           /* CUPIC_FLAG_* raised during the step */
+} cupic_step_stats;
+
+/* ---- parameters -------------------------------------------------------- */
+
+/* Fills *p with the 64x256-cell, 20-particles-per-cell plasma of the small
+ * workload: ds=0.5, dt=0.05, n=160, mi=100, kti=1, phi_p=-5. */
+int cupic_params_default(cupic_params *p);
+
+/* Parses the reference's 13-parameter input_data file (header line then
+ * "name = value;" lines, init.cu:424-447) and normalises it exactly as the
+ * init_* getters do (init.cu:451-789). */
+int cupic_params_from_input_data(const char *path, cupic_params *p);
+
+/* Recomputes derived fields (ppr) after a caller edited *p. */
+int cupic_params_finalize(cupic_params *p);
+
+/* ---- lifetime ---------------------------------------------------------- */
+
+int cupic_create(const cupic_params *p, int device, struct cupic_ctx **out);
+int cupic_destroy(struct cupic_ctx *ctx);
+const char *cupic_strerror(int status);
+
+/* init_sim for n_ini == 0 (init.cu:57-83): seeded uniform/Maxwellian
+ * plasma, linear phi, deposit, initial solve, field, leapfrog half-step. */
+int cupic_init_plasma(struct cupic_ctx *ctx);
+
+/* Replaces one species with n particles given as the reference's particle
+ * struct (4 doubles x,y,vx,vy; stdh.h:30-36), in any order; they are binned
+ * by y row keeping the given order within a row (init.cu:400-407).
+ * Particles outside [0,Lx)x[0,Ly) are rejected with CUPIC_ERR_ARG. */
+int cupic_load_particles(struct cupic_ctx *ctx, int species, const double *xyvv, int64_t n);
+
+/* Sets the simulation clock t and the injection clocks (cc.cu:35-36).
+ * tin < 0 means "first boundary call sets tin = t + dtin". */
+int cupic_set_time(struct cupic_ctx *ctx, int64_t step, double t, double tin_e, double tin_i);
+int cupic_get_time(struct cupic_ctx *ctx, int64_t *step, double *t, double *tin_e, double *tin_i);
+
+/* ---- the cycle (reference entry points) -------------------------------- */
+
+/* Deposits rho from the current particles (only needed after a load). */
+int cupic_charge_deposition(struct cupic_ctx *ctx);
+/* Jacobi solve; max_error<0 uses the per-step parameters of ctx. */
+int cupic_poisson_solver(struct cupic_ctx *ctx, double max_error, int32_t min_sweeps,
+                         int32_t max_sweeps, int32_t check_every);
+int cupic_field_solver(struct cupic_ctx *ctx);
+/* Gather + leapfrog + periodic wrap + y-row binning + probe absorption;
+ * also deposits the moved particles into the next charge accumulator. */
+int cupic_particle_mover(struct cupic_ctx *ctx);
+/* Injection of the half-Maxwellian flux at y=Ly for the step at time t and
+ * end-of-step bookkeeping (cc.cu:134-272). */
+int cupic_cc(struct cupic_ctx *ctx, double t);
+
+/* nsteps full cycles (solve, field, push, bin, absorb, inject) with the
+ * clock advancing by dt per step, replayed from a captured CUDA graph. */
+int cupic_step(struct cupic_ctx *ctx, int32_t nsteps);
+/* Waits for all work of ctx. */
+int cupic_sync(struct cupic_ctx *ctx);
+
+/* ---- results ----------------------------------------------------------- */
+
+int cupic_get_counts(struct cupic_ctx *ctx, int64_t *n_electrons, int64_t *n_ions);
+/* Copies one species in row order as 4 doubles per particle. */
+int cupic_store_particles(struct cupic_ctx *ctx, int species, double *xyvv, int64_t capacity,
+                          int64_t *n_out);
+/* Same, as 4 floats per particle (the device representation). */
+int cupic_store_particles_f32(struct cupic_ctx *ctx, int species, float *xyvv, int64_t capacity,
+                              int64_t *n_out);
+/* Per-row [first,last] index pairs of the row-ordered particle list, -1 for
+ * empty rows: the reference's bookmark array (init.cu:159-165). */
+int cupic_get_bookmarks(struct cupic_ctx *ctx, int species, int32_t *bm);
+/* Mesh arrays, nnx*nny doubles, index i + j*nnx.  which=0: the charge the
+ * next solve will use; which=1: the charge used by the last solve. */
+int cupic_get_rho(struct cupic_ctx *ctx, int which, double *rho);
+int cupic_get_rho_fixed(struct cupic_ctx *ctx, int which, int64_t *acc);
+int cupic_get_phi(struct cupic_ctx *ctx, double *phi);
+int cupic_set_phi(struct cupic_ctx *ctx, const double *phi);
+int cupic_get_field(struct cupic_ctx *ctx, double *ex, double *ey);
+int cupic_get_phi_f32(struct cupic_ctx *ctx, float *phi);
+int cupic_get_field_f32(struct cupic_ctx *ctx, float *ex, float *ey);
+/* Stats of the last `count` steps (most recent last). */
+int cupic_get_stats(struct cupic_ctx *ctx, cupic_step_stats *out, int32_t count);
+int cupic_get_flags(struct cupic_ctx *ctx, uint32_t *flags);
+int cupic_clear_flags(struct cupic_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUPIC_GPU_H */
