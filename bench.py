@@ -1,0 +1,405 @@
+"""Benchmark of the electrostatic PIC cycle (particle-steps/s).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl cupic|reference]
+
+One "step" is one full cycle (Jacobi solve + field, push + binning +
+deposition, injection) of the 512x2048-cell, 100-particles-per-cell
+workload (about 2.1e8 particles).  Rank 0 prints one JSON line.
+
+value      device time of K steps (CUDA events on the library's stream, inputs
+           resident in HBM); particle arrays (3.4 GB) are far larger than L2
+e2e        the same K steps through the public C-ABI from pinned host
+           buffers: upload of both species (the reference's 4-double particle
+           struct), K graph-launched steps each followed by a read of the
+           step's counters, download of both species at the end
+roofline   the dominant kernel's algorithmic bytes per launch / its mean
+           event-timed duration, against the measured HBM copy bandwidth
+cpu_baseline  the CPU oracle (the reference algorithm restated, FP64,
+           OpenMP) on a strip of the same workload, rank 0 only
+--impl reference  the same CPU oracle as the timed arm on the same metric
+
+For N > 1 (torchrun), every rank runs an independent replica on its own GPU
+(no collective on the data path); value sums particle-steps over ranks and
+divides by the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s full PIC cycle"
+UNIT = "particle-steps/s"
+STATS_BYTES = 96
+
+# algorithmic bytes per unit of work (FP32 SoA, 16 B state per particle)
+PUSH_BYTES_PER_PARTICLE = 32      # 16 B read + 16 B write
+PUSH_BYTES_PER_NODE = 16          # E read once (8 B) + int64 charge flush (8 B)
+JACOBI_BYTES_PER_NODE_SWEEP = 12  # phi read, source read, phi write
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["cupic", "reference"], default="cupic")
+    ap.add_argument("--workload", choices=["large", "small", "tiny"], default="large")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ncy", type=int, default=0,
+                    help="override the y cell count (smaller cases for profiling)")
+    ap.add_argument("--cpu-rows", type=int, default=0,
+                    help="rows of the CPU sample strip (0: sized to ~1 s per step)")
+    return ap.parse_args()
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def allmax(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def allsum(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(v)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def workload_desc(p):
+    ppc = p.ppr // p.ncx
+    return (f"{p.ncx}x{p.ncy} cells, ds={p.ds}, {ppc} particles per cell per species, "
+            f"mi/me={p.mi:g}, Ti/Te={p.kti:g}, phi_p={p.phi_p:g}, dt={p.dt:g}, "
+            f"Jacobi {p.min_sweeps}-{p.max_sweeps} sweeps, seed {p.seed}")
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel, units):
+    """dram bytes per launch of `kernel` scaled to `units`, from the committed
+    ncu summary (profiles/ncu_traffic.json), or None."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        d = json.load(f)
+    k = d.get(kernel)
+    if not k:
+        return None
+    return float(k["dram_bytes_per_unit"]) * units
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.15)
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        rows = []
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), float(f[3]) if f[3] not in ("", "[N/A]") else 0.0,
+                             f[5], f[6], f[7], f[8]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        pmax = max(r[2] for r in rows)
+        load = [r for r in rows if r[2] >= 0.5 * pmax] or rows
+        reasons = set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for r in load:
+            for name, v in zip(names, r[3:]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r[0] for r in load), "sm_max_mhz": max(r[1] for r in rows),
+                "samples": len(rows), "samples_under_load": len(load),
+                "power_w_max": pmax, "reasons": sorted(reasons)}
+
+
+# ---------------------------------------------------------------------------
+# CPU oracle (the reference algorithm restated) on a strip of the workload
+# ---------------------------------------------------------------------------
+
+def cpu_strip(p, rows_req, steps, warmup, target_s=1.0):
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    rows = rows_req
+    if rows <= 0:
+        # size the strip so one step takes about target_s on this host
+        probe = p.copy()
+        probe.ncy = 16
+        probe.finalize()
+        o = O.Oracle(probe, fp64=True)
+        o.init_plasma()
+        t0 = time.perf_counter()
+        o.step(1)
+        dt = time.perf_counter() - t0
+        o.close()
+        rows = int(max(16, min(p.ncy, 16 * target_s / max(dt, 1e-4))))
+    q = p.copy()
+    q.ncy = rows
+    q.finalize()
+    o = O.Oracle(q, fp64=True)
+    o.init_plasma()
+    if warmup:
+        o.step(warmup)
+    n0 = sum(o.counts())
+    t0 = time.perf_counter()
+    o.step(steps)
+    el = time.perf_counter() - t0
+    n1 = sum(o.counts())
+    ps = 0.5 * (n0 + n1) * steps
+    sample = (f"FP64 oracle, {q.ncx}x{rows}-row strip of the workload ({n0} particles, "
+              f"{q.max_sweeps} Jacobi sweeps per step), {steps} steps after {warmup} warm-up")
+    return {"value": ps / el, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+            "seconds": el}
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    p = make_params(args)
+    cb = cpu_strip(p, args.cpu_rows, args.steps, args.warmup)
+    line = {
+        "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * cb["seconds"] / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded uniform/Maxwellian plasma (Philox4x32-10)",
+        "config": {"workload": workload_desc(p), "sample": cb["sample"], "parallelism": "cpu"},
+        "impl": "reference",
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def pinned_f64(n):
+    try:
+        import torch
+        t = torch.empty((max(n, 1), 4), dtype=torch.float64, pin_memory=True)
+        return t.numpy(), True
+    except Exception:
+        import numpy as np
+        return np.empty((max(n, 1), 4), dtype=np.float64), False
+
+
+def run_e2e(sim, steps, pinned_state):
+    """K steps through the public C-ABI from and back to host buffers."""
+    import ctypes
+
+    import cupic_gb300 as cg
+    L = sim.L
+    bufs, ns = pinned_state
+    t, tin = sim.get_time()[1], sim.get_time()[2:]
+    step0 = sim.get_time()[0]
+    stats = (cg.StepStats * 1)()
+    h2d = sum(ns) * 32
+    t0 = time.perf_counter()
+    for sp in (0, 1):
+        rc = L.cupic_load_particles(sim.h, sp, bufs[sp].ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                    ns[sp])
+        if rc:
+            raise cg.CupicError(rc, "load")
+    for _ in range(steps):
+        rc = L.cupic_step(sim.h, 1)
+        rc = rc or L.cupic_get_stats(sim.h, stats, 1)
+        if rc:
+            raise cg.CupicError(rc, "step")
+    got = [ctypes.c_int64(), ctypes.c_int64()]
+    out = 0
+    for sp in (0, 1):
+        rc = L.cupic_store_particles(sim.h, sp, bufs[sp].ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                     bufs[sp].shape[0], ctypes.byref(got[sp]))
+        if rc:
+            raise cg.CupicError(rc, "store")
+        out += got[sp].value * 32
+    el = time.perf_counter() - t0
+    return el, h2d, out + steps * STATS_BYTES
+
+
+def make_params(args):
+    from cupic_gb300 import workload_params
+    p = workload_params(args.workload)
+    if args.ncy:
+        p.ncy = args.ncy
+        p.finalize()
+    return p
+
+
+def run_cupic(args, world, rank, local):
+    import cupic_gb300 as cg
+    p = make_params(args)
+    sim = cg.Sim(p, device=local)
+    sim.init_plasma()
+    if args.warmup:
+        sim.step(args.warmup)
+    nodes = p.nnx * p.nny
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(world)
+    total_ms, phases = sim.step_timed(args.steps)
+    barrier(world)
+    clocks = sampler.stop()
+    st = sim.stats(args.steps)
+    flags = 0
+    for s in st:
+        flags |= s["flags"]
+    live = [sum(s["live"]) for s in st]
+    before = [sum(st[0]["live"]) - st[0]["injected"][0] - st[0]["injected"][1]
+              + sum(st[0]["absorbed"]) + sum(st[0]["removed"])] + live[:-1]
+    pstep = float(sum(before))
+    tmax = allmax(total_ms / 1e3, world)
+    ps_all = allsum(pstep, world)
+    value = ps_all / tmax
+    mean_particles = pstep / args.steps
+    sweeps = [s["sweeps"] for s in st]
+
+    peak, peak_kind = measured_peaks()
+    push_ms = phases["push"] / args.steps
+    solve_ms = phases["solve"] / args.steps
+    push_bytes = PUSH_BYTES_PER_PARTICLE * mean_particles + PUSH_BYTES_PER_NODE * nodes
+    jac_bytes = JACOBI_BYTES_PER_NODE_SWEEP * nodes * statistics.mean(sweeps)
+    push_gbs = push_bytes / (push_ms * 1e-3) / 1e9
+    jac_gbs = jac_bytes / (solve_ms * 1e-3) / 1e9
+    roof_push = {"kernel": "k_push_deposit", "bound": "hbm", "achieved": push_gbs, "peak": peak,
+                 "unit": "GB/s", "frac": push_gbs / peak, "peak_source": peak_kind,
+                 "traffic": ncu_traffic("k_push_deposit", mean_particles),
+                 "algorithmic_bytes": push_bytes, "mean_ms": push_ms}
+    roof_jac = {"kernel": "k_jacobi", "bound": "hbm", "achieved": jac_gbs, "peak": peak,
+                "unit": "GB/s", "frac": jac_gbs / peak, "peak_source": peak_kind,
+                "traffic": ncu_traffic("k_jacobi", nodes),
+                "algorithmic_bytes": jac_bytes, "mean_ms": solve_ms,
+                "note": "12 B/node/sweep counted per sweep; the mesh stays on chip"}
+    dominant, other = (roof_push, roof_jac) if push_ms >= solve_ms else (roof_jac, roof_push)
+
+    e2e = None
+    if not args.no_e2e:
+        ns = sim.counts()
+        bufs = []
+        pinned = True
+        for sp in (0, 1):
+            b, pin = pinned_f64(ns[sp])
+            pinned = pinned and pin
+            bufs.append(b)
+            # the state to upload: the current one, as the reference's struct
+            import ctypes
+            got = ctypes.c_int64()
+            sim.L.cupic_store_particles(sim.h, sp, b.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                        b.shape[0], ctypes.byref(got))
+        barrier(world)
+        el, h2d, d2h = run_e2e(sim, args.steps, (bufs, ns))
+        el = allmax(el, world)
+        e2e_ps = allsum(float(sum(ns)) * args.steps, world)
+        e2e = {"value": e2e_ps / el, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
+               "d2h_bytes_per_step": d2h / args.steps, "pinned_host": pinned,
+               "seconds": el}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = cpu_strip(p, args.cpu_rows, steps=8, warmup=1, target_s=1.5)
+        cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded uniform positions, Maxwellian velocities (Philox4x32-10)",
+            "config": {"workload": workload_desc(p), "ncx": p.ncx, "ncy": p.ncy,
+                       "particles_per_step": mean_particles, "nodes": nodes,
+                       "jacobi_sweeps": statistics.mean(sweeps),
+                       "l2": "inputs larger than L2 (particle arrays 3.4 GB); the 4 MB mesh "
+                             "stays L2/shared-memory resident by design",
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "jacobi_ctas": None},
+            "e2e": e2e,
+            "gpu_launches": 6 * args.steps,
+            "roofline": dominant,
+            "roofline_other": other,
+            "phases_ms_per_step": {k: v / args.steps for k, v in phases.items()},
+            "cpu_baseline": cpu,
+            "clocks": clocks,
+            "device_flags": flags,
+        }
+        print(json.dumps(line), flush=True)
+    sim.close()
+    return 0
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+    return run_cupic(args, world, rank, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

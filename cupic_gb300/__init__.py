@@ -29,7 +29,7 @@ EXPORTED = [
     "cupic_create", "cupic_destroy", "cupic_strerror", "cupic_init_plasma",
     "cupic_load_particles", "cupic_set_time", "cupic_get_time",
     "cupic_charge_deposition", "cupic_poisson_solver", "cupic_field_solver",
-    "cupic_particle_mover", "cupic_cc", "cupic_step", "cupic_sync",
+    "cupic_particle_mover", "cupic_cc", "cupic_step", "cupic_sync", "cupic_step_timed",
     "cupic_get_counts", "cupic_store_particles", "cupic_store_particles_f32",
     "cupic_get_bookmarks", "cupic_get_rho", "cupic_get_rho_fixed", "cupic_get_phi",
     "cupic_set_phi", "cupic_get_field", "cupic_get_phi_f32", "cupic_get_field_f32",
@@ -79,6 +79,7 @@ def load_library(build_if_missing=False):
         "cupic_cc": [vp, c_d],
         "cupic_step": [vp, c_i32],
         "cupic_sync": [vp],
+        "cupic_step_timed": [vp, c_i32, P(ctypes.c_float), c_i32, P(ctypes.c_float)],
         "cupic_get_counts": [vp, P(c_i64), P(c_i64)],
         "cupic_store_particles": [vp, c_i, P(c_d), c_i64, P(c_i64)],
         "cupic_store_particles_f32": [vp, c_i, P(ctypes.c_float), c_i64, P(c_i64)],
@@ -202,6 +203,16 @@ class Sim:
         _ok(self.L.cupic_step(self.h, n), "step")
         if sync:
             self.sync()
+
+    PHASES = ("solve", "zero", "push", "arrive", "inject", "final")
+
+    def step_timed(self, n):
+        """n cycles with device timing per phase: (total_ms, {phase: ms})."""
+        ph = (ctypes.c_float * len(self.PHASES))()
+        tot = ctypes.c_float()
+        _ok(self.L.cupic_step_timed(self.h, n, ph, len(self.PHASES), ctypes.byref(tot)),
+            "step_timed")
+        return tot.value, dict(zip(self.PHASES, list(ph)))
 
     def sync(self):
         _ok(self.L.cupic_sync(self.h), "sync")

@@ -305,24 +305,6 @@ int capture_step(cupic_ctx *c) {
   return CUPIC_OK;
 }
 
-struct PackArgs {
-  const float4 *parts;
-  const int64_t *seg;
-  const int64_t *off;  // [ncy+1] packed offsets
-  float4 *packed;
-};
-
-__global__ void k_pack(PackArgs A, int to_rows) {
-  const int j = blockIdx.x;
-  const int64_t o = A.off[j], n = A.off[j + 1] - o;
-  for (int64_t k = threadIdx.x; k < n; k += blockDim.x) {
-    if (to_rows)
-      const_cast<float4 *>(A.parts)[A.seg[j] + k] = A.packed[o + k];
-    else
-      A.packed[o + k] = A.parts[A.seg[j] + k];
-  }
-}
-
 int get_row_counts(cupic_ctx *c, int sp, std::vector<int32_t> &cnt) {
   cnt.resize(c->p.ncy);
   CU(cudaStreamSynchronize(c->stream));
@@ -330,34 +312,38 @@ int get_row_counts(cupic_ctx *c, int sp, std::vector<int32_t> &cnt) {
   return CUPIC_OK;
 }
 
-// copy species sp to a packed device array, return it (caller frees)
-int pack_species(cupic_ctx *c, int sp, float4 **out, int64_t *n) {
+// species sp in row order into host memory, as float4 (out32) or as the
+// reference's 4-double struct (out64), with one device-to-host copy
+int store_species(cupic_ctx *c, int sp, float *out32, double *out64, int64_t capacity,
+                  int64_t *n_out) {
   std::vector<int32_t> cnt;
   int rc = get_row_counts(c, sp, cnt);
   if (rc) return rc;
   const int ncy = c->p.ncy;
   std::vector<int64_t> off(ncy + 1, 0);
   for (int j = 0; j < ncy; ++j) off[j + 1] = off[j] + cnt[j];
-  *n = off[ncy];
+  const int64_t n = off[ncy];
+  if (n_out) *n_out = n;
+  if (n > capacity || (n > 0 && !out32 && !out64)) return CUPIC_ERR_ARG;
+  if (n == 0) return CUPIC_OK;
+  const size_t bytes = (size_t)n * (out64 ? 32 : 16);
   int64_t *doff = nullptr;
-  float4 *packed = nullptr;
+  void *packed = nullptr;
   CU(dalloc(&doff, ncy + 1));
-  cudaError_t e = dalloc(&packed, (size_t)std::max<int64_t>(*n, 1));
-  if (e != cudaSuccess) {
-    cudaFree(doff);
-    return cuda_status(e);
-  }
-  CU(cudaMemcpy(doff, off.data(), (ncy + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
-  PackArgs A{c->a.sp[sp].parts, c->a.sp[sp].seg, doff, packed};
-  k_pack<<<ncy, 256, 0, c->stream>>>(A, 0);
-  e = cudaStreamSynchronize(c->stream);
+  cudaError_t e = cudaMalloc(&packed, bytes);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(doff, off.data(), (ncy + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
+                        c->stream);
+  if (e == cudaSuccess)
+    e = launch_pack_rows(c->a, sp, doff, out64 ? nullptr : (float4 *)packed,
+                         out64 ? (double *)packed : nullptr, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(out64 ? (void *)out64 : (void *)out32, packed, bytes,
+                        cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   cudaFree(doff);
-  if (e != cudaSuccess) {
-    cudaFree(packed);
-    return cuda_status(e);
-  }
-  *out = packed;
-  return CUPIC_OK;
+  cudaFree(packed);
+  return e == cudaSuccess ? CUPIC_OK : cuda_status(e);
 }
 
 bool read_line(const char *path, int n, char *line, size_t cap) {
@@ -613,53 +599,54 @@ int cupic_init_plasma(cupic_ctx *c) {
 int cupic_load_particles(cupic_ctx *c, int sp, const double *xyvv, int64_t n) {
   if (!c || sp < 0 || sp > 1 || n < 0 || (n > 0 && !xyvv)) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
+  CU(cudaStreamSynchronize(c->stream));
   const int ncy = c->p.ncy;
-  const float inv_ds = c->a.inv_ds, Lx = c->a.Lx, Ly = c->a.Ly;
+  const int nb = load_blocks(n, c->num_sms);
+  double *din = nullptr;
+  float4 *tmp = nullptr;
+  int32_t *H = nullptr;
+  unsigned *bad = nullptr;
   std::vector<int32_t> cnt(ncy, 0);
-  std::vector<int32_t> rowk((size_t)n);
-  for (int64_t k = 0; k < n; ++k) {
-    const float x = (float)xyvv[4 * k], y = (float)xyvv[4 * k + 1];
-    if (!(x >= 0.0f && x < Lx && y >= 0.0f && y < Ly)) return CUPIC_ERR_ARG;
-    const float sy = y * inv_ds;
-    int j = (int)floorf(sy);
-    j = j < 0 ? 0 : (j > ncy - 1 ? ncy - 1 : j);
-    rowk[k] = j;
-    cnt[j]++;
-  }
-  std::vector<int64_t> off(ncy + 1, 0);
-  for (int j = 0; j < ncy; ++j) off[j + 1] = off[j] + cnt[j];
-  std::vector<float4> packed((size_t)std::max<int64_t>(n, 1));
-  std::vector<int64_t> fill(off.begin(), off.end() - 1);
-  for (int64_t k = 0; k < n; ++k) {
-    packed[fill[rowk[k]]++] = make_float4((float)xyvv[4 * k], (float)xyvv[4 * k + 1],
-                                          (float)xyvv[4 * k + 2], (float)xyvv[4 * k + 3]);
-  }
-  bool grow = false;
-  std::vector<int32_t> capv = c->cap[sp];
-  for (int j = 0; j < ncy; ++j)
-    if (cnt[j] > capv[j]) {
-      capv[j] = round8(cnt[j] * (1.0 + c->p.row_slack)) + 64;
-      grow = true;
+  unsigned hbad = 0;
+  int rc = CUPIC_OK;
+  cudaError_t e = dalloc(&din, (size_t)4 * n);
+  if (e == cudaSuccess) e = dalloc(&tmp, (size_t)n);
+  if (e == cudaSuccess) e = dalloc(&H, (size_t)nb * ncy);
+  if (e == cudaSuccess) e = dalloc(&bad, 1);
+  if (e == cudaSuccess) e = cudaMemsetAsync(bad, 0, sizeof(unsigned), c->stream);
+  if (e == cudaSuccess && n > 0)
+    e = cudaMemcpyAsync(din, xyvv, (size_t)n * 32, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess && n > 0) e = launch_load_hist(c->a, din, n, nb, tmp, H, bad, c->stream);
+  if (e == cudaSuccess && n > 0) e = launch_load_scan(H, nb, ncy, c->a.sp[sp].cnt, c->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&hbad, bad, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess && n > 0)
+    e = cudaMemcpyAsync(cnt.data(), c->a.sp[sp].cnt, ncy * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                        c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) rc = cuda_status(e);
+  if (!rc && hbad) rc = CUPIC_ERR_ARG;
+  if (!rc) {
+    bool grow = false;
+    std::vector<int32_t> capv = c->cap[sp];
+    for (int j = 0; j < ncy; ++j)
+      if (cnt[j] > capv[j]) {
+        capv[j] = round8(cnt[j] * (1.0 + c->p.row_slack)) + 64;
+        grow = true;
+      }
+    if (grow) rc = layout_species(c, sp, capv);
+    if (!rc) {
+      e = cudaMemcpyAsync(c->a.sp[sp].cnt, cnt.data(), ncy * sizeof(int32_t),
+                          cudaMemcpyHostToDevice, c->stream);
+      if (e == cudaSuccess && n > 0) e = launch_load_scatter(c->a, sp, tmp, n, nb, H, c->stream);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+      if (e != cudaSuccess) rc = cuda_status(e);
     }
-  CU(cudaStreamSynchronize(c->stream));
-  if (grow) {
-    int rc = layout_species(c, sp, capv);
-    if (rc) return rc;
   }
-  SpeciesDev &S = c->a.sp[sp];
-  int64_t *doff = nullptr;
-  float4 *dp = nullptr;
-  CU(dalloc(&doff, ncy + 1));
-  CU(dalloc(&dp, packed.size()));
-  CU(cudaMemcpy(doff, off.data(), (ncy + 1) * sizeof(int64_t), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(dp, packed.data(), packed.size() * sizeof(float4), cudaMemcpyHostToDevice));
-  PackArgs A{S.parts, S.seg, doff, dp};
-  k_pack<<<ncy, 256, 0, c->stream>>>(A, 1);
-  CU(cudaGetLastError());
-  CU(cudaMemcpyAsync(S.cnt, cnt.data(), ncy * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream));
-  CU(cudaStreamSynchronize(c->stream));
-  cudaFree(doff);
-  cudaFree(dp);
+  cudaFree(din);
+  cudaFree(tmp);
+  cudaFree(H);
+  cudaFree(bad);
+  if (rc) return rc;
   c->rho_valid = false;
   c->initialized = true;
   return CUPIC_OK;
@@ -771,34 +758,72 @@ int cupic_get_counts(cupic_ctx *c, int64_t *ne, int64_t *ni) {
 int cupic_store_particles_f32(cupic_ctx *c, int sp, float *out, int64_t capacity, int64_t *n_out) {
   if (!c || sp < 0 || sp > 1) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
-  float4 *packed = nullptr;
-  int64_t n = 0;
-  int rc = pack_species(c, sp, &packed, &n);
-  if (rc) return rc;
-  if (n_out) *n_out = n;
-  if (n > capacity || (n > 0 && !out)) {
-    cudaFree(packed);
-    return CUPIC_ERR_ARG;
-  }
-  cudaError_t e = cudaMemcpy(out, packed, (size_t)n * sizeof(float4), cudaMemcpyDeviceToHost);
-  cudaFree(packed);
-  return e == cudaSuccess ? CUPIC_OK : cuda_status(e);
+  return store_species(c, sp, out, nullptr, capacity, n_out);
 }
 
 int cupic_store_particles(cupic_ctx *c, int sp, double *out, int64_t capacity, int64_t *n_out) {
   if (!c || sp < 0 || sp > 1) return CUPIC_ERR_ARG;
-  int64_t ne = 0, ni = 0;
-  int rc = cupic_get_counts(c, &ne, &ni);
-  if (rc) return rc;
-  const int64_t n = sp == 0 ? ne : ni;
-  if (n_out) *n_out = n;
-  if (n > capacity || (n > 0 && !out)) return CUPIC_ERR_ARG;
-  std::vector<float> tmp((size_t)std::max<int64_t>(4 * n, 4));
-  int64_t got = 0;
-  rc = cupic_store_particles_f32(c, sp, tmp.data(), n, &got);
-  if (rc) return rc;
-  for (int64_t k = 0; k < 4 * got; ++k) out[k] = (double)tmp[k];
-  return CUPIC_OK;
+  CU(cudaSetDevice(c->device));
+  if (!out) {
+    std::vector<int32_t> cnt;
+    int rc = get_row_counts(c, sp, cnt);
+    if (rc) return rc;
+    int64_t n = 0;
+    for (int32_t v : cnt) n += v;
+    if (n_out) *n_out = n;
+    return n == 0 ? CUPIC_OK : CUPIC_ERR_ARG;
+  }
+  return store_species(c, sp, nullptr, out, capacity, n_out);
+}
+
+int cupic_step_timed(cupic_ctx *c, int32_t nsteps, float *phase_ms, int32_t nphase,
+                     float *total_ms) {
+  if (!c || nsteps < 1 || !phase_ms || nphase < CUPIC_NPHASE || !total_ms) return CUPIC_ERR_ARG;
+  if (!c->initialized) return CUPIC_ERR_STATE;
+  CU(cudaSetDevice(c->device));
+  if (!c->rho_valid) {
+    int rc = deposit_current(c);
+    if (rc) return rc;
+  }
+  const int per = CUPIC_NPHASE;
+  std::vector<cudaEvent_t> ev((size_t)nsteps * per + 1, nullptr);
+  int rc = CUPIC_OK;
+  for (auto &e : ev)
+    if (cudaEventCreate(&e) != cudaSuccess) rc = CUPIC_ERR_CUDA;
+  const cupic_params &p = c->p;
+  const JacobiArgs J = jargs(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1);
+  cudaError_t e = rc ? cudaErrorUnknown : cudaEventRecord(ev[0], c->stream);
+  for (int s = 0; s < nsteps && e == cudaSuccess; ++s) {
+    cudaEvent_t *q = &ev[(size_t)s * per + 1];
+    e = launch_jacobi(c->a, J, c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(q[0], c->stream);
+    if (e == cudaSuccess) e = launch_zero_next_rho(c->a, c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(q[1], c->stream);
+    if (e == cudaSuccess) e = launch_push_deposit(c->a, c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(q[2], c->stream);
+    if (e == cudaSuccess) e = launch_arrive(c->a, c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(q[3], c->stream);
+    if (e == cudaSuccess) e = launch_inject(c->a, c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(q[4], c->stream);
+    if (e == cudaSuccess) e = launch_finalize(c->a, c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(q[5], c->stream);
+    if (e == cudaSuccess) c->host_cur ^= 1;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  for (int k = 0; k < nphase; ++k) phase_ms[k] = 0.0f;
+  if (e == cudaSuccess) {
+    for (int s = 0; s < nsteps && e == cudaSuccess; ++s)
+      for (int k = 0; k < per && e == cudaSuccess; ++k) {
+        float ms = 0.0f;
+        e = cudaEventElapsedTime(&ms, ev[(size_t)s * per + k], ev[(size_t)s * per + k + 1]);
+        phase_ms[k] += ms;
+      }
+    if (e == cudaSuccess) e = cudaEventElapsedTime(total_ms, ev[0], ev.back());
+  }
+  for (auto &x : ev)
+    if (x) cudaEventDestroy(x);
+  if (e != cudaSuccess) return rc ? rc : cuda_status(e);
+  return finish(c);
 }
 
 int cupic_get_bookmarks(cupic_ctx *c, int sp, int32_t *bm) {

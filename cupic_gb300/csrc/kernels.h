@@ -19,6 +19,15 @@ cudaError_t launch_finalize(const SimArgs &a, cudaStream_t st);
 size_t push_smem_bytes(int nnx);
 cudaError_t push_set_smem(size_t bytes);
 
+int load_blocks(int64_t n, int num_sms);
+cudaError_t launch_load_hist(const SimArgs &a, const double *in, int64_t n, int nb, float4 *tmp,
+                             int32_t *H, unsigned *bad, cudaStream_t st);
+cudaError_t launch_load_scan(int32_t *H, int nb, int ncy, int32_t *cnt, cudaStream_t st);
+cudaError_t launch_load_scatter(const SimArgs &a, int sp, const float4 *tmp, int64_t n, int nb,
+                                const int32_t *H, cudaStream_t st);
+cudaError_t launch_pack_rows(const SimArgs &a, int sp, const int64_t *off, float4 *out32,
+                             double *out64, cudaStream_t st);
+
 size_t jacobi_smem_bytes(int rows_per_cta, int pitch);
 int jacobi_block();
 cudaError_t jacobi_set_smem(size_t bytes);

@@ -168,6 +168,22 @@ int cupic_step(struct cupic_ctx *ctx, int32_t nsteps);
 /* Waits for all work of ctx. */
 int cupic_sync(struct cupic_ctx *ctx);
 
+/* Phases of a step, for cupic_step_timed. */
+enum {
+  CUPIC_PHASE_SOLVE = 0,  /* Jacobi sweeps + field (mesh.cu:55-154) */
+  CUPIC_PHASE_ZERO = 1,   /* clearing the next charge accumulator (mesh.cu:35) */
+  CUPIC_PHASE_PUSH = 2,   /* push + wrap + binning + deposition (particles.cu, cc.cu, mesh.cu) */
+  CUPIC_PHASE_ARRIVE = 3, /* movers appended to their new rows (cc.cu:640-772) */
+  CUPIC_PHASE_INJECT = 4, /* injected flux (cc.cu:134-272) */
+  CUPIC_PHASE_FINAL = 5,  /* per-step counters and clock */
+  CUPIC_NPHASE = 6
+};
+/* nsteps cycles launched one kernel at a time with a CUDA event between
+ * kernels on the context's stream; phase_ms[k] = device ms of phase k summed
+ * over the steps, *total_ms = device ms from the first to the last event. */
+int cupic_step_timed(struct cupic_ctx *ctx, int32_t nsteps, float *phase_ms, int32_t nphase,
+                     float *total_ms);
+
 /* ---- results ----------------------------------------------------------- */
 
 int cupic_get_counts(struct cupic_ctx *ctx, int64_t *n_electrons, int64_t *n_ions);
