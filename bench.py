@@ -36,6 +36,8 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s full PIC cycle"
 UNIT = "particle-steps/s"
 STATS_BYTES = 96
+# kernels launched per step: jacobi, zero, push, arrive, inject sched/gen/append, finalize
+KERNELS_PER_STEP = 8
 
 # algorithmic bytes per unit of work (FP32 SoA, 16 B state per particle)
 PUSH_BYTES_PER_PARTICLE = 32      # 16 B read + 16 B write
@@ -54,6 +56,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncy", type=int, default=0,
                     help="override the y cell count (smaller cases for profiling)")
+    ap.add_argument("--ppc", type=float, default=0,
+                    help="override particles per cell per species (profiling the mesh solve)")
     ap.add_argument("--cpu-rows", type=int, default=0,
                     help="rows of the CPU sample strip (0: sized to ~1 s per step)")
     return ap.parse_args()
@@ -289,7 +293,10 @@ def make_params(args):
     p = workload_params(args.workload)
     if args.ncy:
         p.ncy = args.ncy
-        p.finalize()
+    if args.ppc:
+        p.n = args.ppc / p.ds ** 3
+        p.eps0 = p.n
+    p.finalize()
     return p
 
 
@@ -380,7 +387,7 @@ def run_cupic(args, world, rank, local):
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "jacobi_ctas": None},
             "e2e": e2e,
-            "gpu_launches": 6 * args.steps,
+            "gpu_launches": KERNELS_PER_STEP * args.steps,
             "roofline": dominant,
             "roofline_other": other,
             "phases_ms_per_step": {k: v / args.steps for k, v in phases.items()},

@@ -29,7 +29,7 @@ struct cupic_ctx {
   std::vector<int32_t> cap[2];
   int64_t total_cap[2] = {0, 0};
   // Jacobi geometry and exchange buffers
-  int jG = 1, jB = 1, jP = 0;
+  int jG = 1, jB = 1, jK = 1, jP = 0;
   unsigned *jflags = nullptr;  // [G+1]: per-CTA sweep counters, then the barrier
   float *jres = nullptr;
   float *jhalo = nullptr;
@@ -78,6 +78,8 @@ void free_species(SpeciesDev &S) {
   cudaFree(S.stage_up);
   cudaFree(S.stage_down);
   cudaFree(S.inj_tin);
+  cudaFree(S.inj_p);
+  cudaFree(S.inj_d);
   memset(&S, 0, sizeof(S));
 }
 
@@ -115,6 +117,8 @@ int layout_species(cupic_ctx *c, int sp, const std::vector<int32_t> &capv) {
   CU(dalloc(&S.stage_up, (size_t)ncy * S.stage_cap));
   CU(dalloc(&S.stage_down, (size_t)ncy * S.stage_cap));
   CU(dalloc(&S.inj_tin, (size_t)S.inj_cap));
+  CU(dalloc(&S.inj_p, (size_t)S.inj_cap));
+  CU(dalloc(&S.inj_d, (size_t)S.inj_cap));
   CU(cudaMemcpy(S.seg, c->seg[sp].data(), ncy * sizeof(int64_t), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(S.cap, capv.data(), ncy * sizeof(int32_t), cudaMemcpyHostToDevice));
   CU(cudaMemset(S.cnt, 0, ncy * sizeof(int32_t)));
@@ -169,37 +173,53 @@ void fill_constants(cupic_ctx *c) {
   a.k1 = (uint32_t)(p.seed >> 32);
 }
 
+// Jacobi geometry: G CTAs of 1024 threads, each holding its rows (+ halos)
+// in shared memory.  Small meshes run in one CTA (no inter-CTA traffic at
+// all); larger ones spread over the SMs with temporal blocking depth K.
+// CUPIC_JACOBI_CTAS / CUPIC_JACOBI_DEPTH override the choice (tuning).
 int plan_jacobi(cupic_ctx *c) {
   const int M = c->a.nny - 2, nnx = c->a.nnx;
   int dev_max = 0;
   CU(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
   const int P = nnx;
   const size_t avail = (size_t)dev_max - 1024;  // static shared memory of the kernel
-  int bmax = (int)((avail / (sizeof(float) * (size_t)P) - 4) / 3);
-  if (bmax < 1) return CUPIC_ERR_ARG;
-  int G, B;
+  const long long rows_fit = (long long)(avail / (3 * sizeof(float) * (size_t)P));
   const char *env = getenv("CUPIC_JACOBI_CTAS");
-  const int forced = env ? atoi(env) : 0;
-  if (forced > 0) {
-    B = std::max(1, (M + forced - 1) / forced);
-  } else if (M <= bmax && (long long)M * nnx <= 65536) {
-    B = M;
-  } else {
-    B = std::max(1, (M + c->num_sms - 1) / c->num_sms);
+  const char *envk = getenv("CUPIC_JACOBI_DEPTH");
+  int G = env ? atoi(env) : 0;
+  int K = envk ? atoi(envk) : 0;
+  if (G <= 0) {
+    if (M + 2 <= rows_fit && (long long)M * nnx <= 65536)
+      G = 1;
+    else
+      G = std::min(c->num_sms, M);
   }
-  B = std::min(B, bmax);
-  G = (M + B - 1) / B;
-  const size_t sm = jacobi_smem_bytes(B, P);
+  G = std::max(1, std::min(G, M));
+  int B = (M + G - 1) / G;
+  if (K <= 0) K = 4;
+  K = std::max(1, std::min(K, M / G));
+  if (G == 1) K = 1;
+  while (G > 1 && B + 2 * K > rows_fit) {  // shrink the depth, then add CTAs
+    if (K > 1) {
+      --K;
+    } else {
+      ++G;
+      B = (M + G - 1) / G;
+    }
+  }
+  if (B + 2 * K > rows_fit) return CUPIC_ERR_ARG;
+  const size_t sm = jacobi_smem_bytes(B, K, P);
   CU(jacobi_set_smem(sm));
   int per_sm = 0;
   CU(jacobi_max_ctas(sm, &per_sm));
   if (per_sm < 1 || G > per_sm * c->num_sms) return CUPIC_ERR_ARG;
   c->jG = G;
   c->jB = B;
+  c->jK = K;
   c->jP = P;
   CU(dalloc(&c->jflags, (size_t)G + 1));
   CU(dalloc(&c->jres, (size_t)2 * G));
-  CU(dalloc(&c->jhalo, (size_t)2 * G * 2 * P));
+  CU(dalloc(&c->jhalo, (size_t)2 * G * 2 * K * P));
   return CUPIC_OK;
 }
 
@@ -211,6 +231,7 @@ JacobiArgs jargs(const cupic_ctx *c, double tol, int mn, int mx, int chk, int fi
   J.check_every = chk < 1 ? 1 : chk;
   J.G = c->jG;
   J.rows_per_cta = c->jB;
+  J.depth = c->jK;
   J.pitch = c->jP;
   J.do_field = field;
   J.write_stats = 1;

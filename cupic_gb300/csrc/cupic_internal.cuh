@@ -31,6 +31,7 @@ struct Ctl {
   int32_t sweeps;         // Jacobi sweeps of the last solve
   float residual;         // max |dphi| of its last checked sweep
   int32_t inj_count[2];   // injected this step
+  int32_t inj_gen[2];     // draws generated this step (inj_count capped at inj_cap)
   unsigned long long absorbed[2];
   unsigned long long removed[2];
   int32_t abort;          // a bounded wait gave up: kernels bail out
@@ -53,6 +54,8 @@ struct SpeciesDev {
   int32_t stage_cap;
   int32_t inj_cap;        // most particles injected per step
   double *inj_tin;        // [inj_cap] scratch: injection time of each draw
+  float4 *inj_p;          // [inj_cap] scratch: the injected particles of the step
+  int32_t *inj_d;         // [inj_cap] scratch: their rows (< 0: removed)
 };
 
 // Everything a kernel needs, passed by value.
@@ -79,14 +82,15 @@ struct JacobiArgs {
   double tol;
   int32_t min_sweeps, max_sweeps, check_every;
   int32_t G;              // CTAs (cooperative)
-  int32_t rows_per_cta;   // interior rows owned by one CTA (last may own fewer)
+  int32_t rows_per_cta;   // most interior rows owned by one CTA: ceil((nny-2)/G)
+  int32_t depth;          // temporal blocking: sweeps between halo exchanges (G > 1)
   int32_t pitch;          // smem row pitch in floats
   int32_t do_field;       // 1: derive E after the last sweep
   int32_t write_stats;    // 1: store sweeps/residual in the control block
   unsigned int *flags;    // [G] last sweep published by each CTA
   unsigned int *bar;      // [1] grid barrier counter
   float *res_cta;         // [2*G] per-CTA max |dphi| of a checked sweep
-  float *halo;            // [2 parity][G][2 rows][pitch]
+  float *halo;            // [2 parity][G][2 sides][depth rows][pitch]
 };
 
 // ---------------------------------------------------------------------------
@@ -254,6 +258,56 @@ __device__ __forceinline__ CicFixed cic_fixed(const SimArgs &a, float x, float y
   r.w01 = GX * FY;
   r.w11 = FX * FY;
   return r;
+}
+
+// ---------------------------------------------------------------------------
+// bulk-copy (TMA) + mbarrier helpers, inline PTX (sm_90+; used on sm_103a)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+
+// make the initialised barriers visible to the bulk-copy (async) proxy
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// 1-D bulk copy global -> shared; completion is signalled on bar.
+// dst, src 16-byte aligned; bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// bounded wait for phase `parity` of bar; false if it gave up
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+  const uint32_t a = smem_addr(bar);
+  for (int it = 0; it < (1 << 20); ++it) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+  }
+  return false;
 }
 
 __device__ __forceinline__ bool finite4(const float4 &p) {

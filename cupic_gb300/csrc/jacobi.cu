@@ -62,31 +62,43 @@ __device__ __forceinline__ float block_max(float v, float *red) {
 
 }  // namespace
 
-__global__ void __launch_bounds__(kJBlock) k_jacobi(SimArgs a, JacobiArgs J) {
+// Rows of CTA c: interior rows [r0, r1) with r0 = 1 + c*M/G (M = nny-2), so
+// every CTA owns floor(M/G) or ceil(M/G) rows.  With temporal blocking depth
+// k, a CTA also holds k halo rows on each side; sweep m (1..k) after an
+// exchange updates the rows [r0-k+m, r1+k-m) -- the halo part redundantly,
+// with the same operands as the neighbour, so the values are identical --
+// and the neighbours trade their k boundary rows only every k sweeps.
+__global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) {
   extern __shared__ float jsm[];
   __shared__ float red[33];
   __shared__ int bail;
   const int c = blockIdx.x, G = J.G, tid = threadIdx.x;
-  const int nnx = a.nnx, P = J.pitch, Bm = J.rows_per_cta;
-  const int r0 = 1 + c * Bm;
-  const int r1 = min(r0 + Bm, a.nny - 1);
-  const int B = r1 - r0;
-  float *buf[2] = {jsm, jsm + (size_t)(Bm + 2) * P};
-  float *bsrc = jsm + (size_t)2 * (Bm + 2) * P;
+  const int nnx = a.nnx, nny = a.nny, P = J.pitch;
+  const int M = nny - 2;
+  const int K = G > 1 ? J.depth : 1;
+  const int r0 = 1 + (int)(((long long)c * M) / G);
+  const int r1 = 1 + (int)(((long long)(c + 1) * M) / G);
+  const int lo = max(0, r0 - K);             // first buffered row
+  const int hi = min(nny - 1, r1 - 1 + K);   // last buffered row
+  const int nrows = hi - lo + 1;
+  const int cap = J.rows_per_cta + 2 * K;    // buffer rows reserved per array
+  float *buf[2] = {jsm, jsm + (size_t)cap * P};
+  float *bsrc = jsm + (size_t)2 * cap * P;   // same row indexing as buf
   Ctl *ctl = a.ctl;
   if (tid == 0) bail = 0;
 
-  // phi rows r0-1 .. r1 into both buffers; source term of the owned rows
-  for (int k = tid; k < (B + 2) * nnx; k += kJBlock) {
+  for (int k = tid; k < nrows * nnx; k += kJBlock) {
     const int lr = k / nnx, i = k - lr * nnx;
-    const float v = a.phi[(size_t)(r0 - 1 + lr) * nnx + i];
+    const float v = a.phi[(size_t)(lo + lr) * nnx + i];
     buf[0][lr * P + i] = v;
     buf[1][lr * P + i] = v;
   }
   const long long *acc = reinterpret_cast<const long long *>(a.rho[ctl->cur]);
-  for (int k = tid; k < B * nnx; k += kJBlock) {
+  for (int k = tid; k < nrows * nnx; k += kJBlock) {
     const int lr = k / nnx, i = k - lr * nnx;
-    const size_t rb = (size_t)(r0 + lr) * nnx;
+    const int j = lo + lr;
+    if (j < 1 || j > nny - 2) continue;
+    const size_t rb = (size_t)j * nnx;
     const long long f = (i == 0 || i == nnx - 1) ? acc[rb] + acc[rb + nnx - 1] : acc[rb + i];
     bsrc[lr * P + i] = __double2float_rn((double)f * a.cb);
   }
@@ -99,47 +111,61 @@ __global__ void __launch_bounds__(kJBlock) k_jacobi(SimArgs a, JacobiArgs J) {
     const float *S = buf[src];
     float *D = buf[src ^ 1];
     const bool check = (s % J.check_every == 0) || (s == J.max_sweeps);
+    const int m = G > 1 ? ((s - 1) % K) + 1 : 1;
+    const int u0 = max(1, r0 - K + m) - lo;          // updated local rows [u0, u1)
+    const int u1 = min(nny - 2, r1 - 1 + K - m) + 1 - lo;
+    const int o0 = r0 - lo, o1 = r1 - lo;            // owned local rows
     float md = 0.0f;
-    for (int k = tid; k < B * W; k += kJBlock) {
-      const int lr = k / W + 1, i = k - (lr - 1) * W;
+    const int nu = (u1 - u0) * W;
+    for (int k = tid; k < nu; k += kJBlock) {
+      const int lr = k / W + u0, i = k - (lr - u0) * W;
       const float *cr = S + lr * P;
       const float wv = (i == 0) ? cr[W - 1] : cr[i - 1];
       const float v = __fmul_rn(
           0.25f,
-          __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(bsrc[(lr - 1) * P + i], wv), cr[i + 1]), cr[P + i]),
+          __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(bsrc[lr * P + i], wv), cr[i + 1]), cr[P + i]),
                     cr[i - P]));
       D[lr * P + i] = v;
-      if (check) md = fmaxf(md, fabsf(__fsub_rn(v, cr[i])));
+      const bool own = check && lr >= o0 && lr < o1;
+      if (own) md = fmaxf(md, fabsf(__fsub_rn(v, cr[i])));
       if (i == 0) {
         D[lr * P + W] = v;
-        if (check) md = fmaxf(md, fabsf(__fsub_rn(v, cr[W])));
+        if (own) md = fmaxf(md, fabsf(__fsub_rn(v, cr[W])));
       }
     }
     __syncthreads();
-    if (G > 1) {
-      float *hp = J.halo + ((size_t)(s & 1) * G + c) * 2 * P;
-      for (int i = tid; i < nnx; i += kJBlock) {
-        __stcg(hp + i, D[P + i]);
-        __stcg(hp + P + i, D[B * P + i]);
+    if (G > 1 && m == K) {
+      const int e = s / K;  // exchange number
+      float *hp = J.halo + ((size_t)(e & 1) * G + c) * 2 * K * P;
+      for (int k = tid; k < K * nnx; k += kJBlock) {
+        const int r = k / nnx, i = k - r * nnx;
+        __stcg(hp + r * P + i, D[(o0 + r) * P + i]);
+        __stcg(hp + (K + r) * P + i, D[(o1 - K + r) * P + i]);
       }
       __syncthreads();
       if (tid == 0) {
         __threadfence();
-        st_release(&J.flags[c], (unsigned)s);
+        st_release(&J.flags[c], (unsigned)e);
         bool ok = true;
-        if (c > 0) ok = wait_geq(&J.flags[c - 1], (unsigned)s, ctl);
-        if (ok && c < G - 1) ok = wait_geq(&J.flags[c + 1], (unsigned)s, ctl);
+        if (c > 0) ok = wait_geq(&J.flags[c - 1], (unsigned)e, ctl);
+        if (ok && c < G - 1) ok = wait_geq(&J.flags[c + 1], (unsigned)e, ctl);
         if (!ok) bail = 1;
       }
       __syncthreads();
       if (bail) break;
-      if (c > 0) {
-        const float *hn = J.halo + ((size_t)(s & 1) * G + (c - 1)) * 2 * P + P;
-        for (int i = tid; i < nnx; i += kJBlock) D[i] = __ldcg(hn + i);
+      if (c > 0) {  // rows [r0-K, r0) = the lower neighbour's last K rows
+        const float *hn = J.halo + ((size_t)(e & 1) * G + (c - 1)) * 2 * K * P + K * P;
+        for (int k = tid; k < K * nnx; k += kJBlock) {
+          const int r = k / nnx, i = k - r * nnx;
+          D[(o0 - K + r) * P + i] = __ldcg(hn + r * P + i);
+        }
       }
-      if (c < G - 1) {
-        const float *hn = J.halo + ((size_t)(s & 1) * G + (c + 1)) * 2 * P;
-        for (int i = tid; i < nnx; i += kJBlock) D[(B + 1) * P + i] = __ldcg(hn + i);
+      if (c < G - 1) {  // rows [r1, r1+K) = the upper neighbour's first K rows
+        const float *hn = J.halo + ((size_t)(e & 1) * G + (c + 1)) * 2 * K * P;
+        for (int k = tid; k < K * nnx; k += kJBlock) {
+          const int r = k / nnx, i = k - r * nnx;
+          D[(o1 + r) * P + i] = __ldcg(hn + r * P + i);
+        }
       }
       __syncthreads();
     }
@@ -166,15 +192,18 @@ __global__ void __launch_bounds__(kJBlock) k_jacobi(SimArgs a, JacobiArgs J) {
     }
   }
 
-  // write back the owned rows; derive E = -grad phi (mesh.cu:413-468)
+  // write back the owned rows; derive E = -grad phi (mesh.cu:413-468).  The
+  // rows r0-1 and r1 are current: either just exchanged or updated in the
+  // last sweep of an unfinished temporal block.
   const float *F = buf[src];
-  for (int k = tid; k < B * nnx; k += kJBlock) {
-    const int lr = k / nnx + 1, i = k - (lr - 1) * nnx;
-    a.phi[(size_t)(r0 + lr - 1) * nnx + i] = F[lr * P + i];
+  const int o0 = r0 - lo, o1 = r1 - lo;
+  for (int k = tid; k < (o1 - o0) * nnx; k += kJBlock) {
+    const int lr = k / nnx + o0, i = k - (lr - o0) * nnx;
+    a.phi[(size_t)(lo + lr) * nnx + i] = F[lr * P + i];
   }
   if (J.do_field) {
-    for (int k = tid; k < B * nnx; k += kJBlock) {
-      const int lr = k / nnx + 1, i = k - (lr - 1) * nnx;
+    for (int k = tid; k < (o1 - o0) * nnx; k += kJBlock) {
+      const int lr = k / nnx + o0, i = k - (lr - o0) * nnx;
       const float *cr = F + lr * P;
       const bool seam = (i == 0 || i == nnx - 1);
       const float wv = seam ? cr[nnx - 2] : cr[i - 1];
@@ -182,16 +211,17 @@ __global__ void __launch_bounds__(kJBlock) k_jacobi(SimArgs a, JacobiArgs J) {
       float2 e;
       e.x = __fdiv_rn(__fsub_rn(wv, ev), a.two_ds);
       e.y = __fdiv_rn(__fsub_rn(cr[i - P], cr[i + P]), a.two_ds);
-      a.E[(size_t)(r0 + lr - 1) * nnx + i] = e;
+      a.E[(size_t)(lo + lr) * nnx + i] = e;
     }
     if (c == 0) {
       for (int i = tid; i < nnx; i += kJBlock)
         a.E[i] = make_float2(0.0f, __fdiv_rn(__fsub_rn(F[i], F[P + i]), a.ds));
     }
     if (c == G - 1) {
+      const int t = (nny - 1) - lo;
       for (int i = tid; i < nnx; i += kJBlock)
-        a.E[(size_t)(a.nny - 1) * nnx + i] =
-            make_float2(0.0f, __fdiv_rn(__fsub_rn(F[B * P + i], F[(B + 1) * P + i]), a.ds));
+        a.E[(size_t)(nny - 1) * nnx + i] =
+            make_float2(0.0f, __fdiv_rn(__fsub_rn(F[(t - 1) * P + i], F[t * P + i]), a.ds));
     }
   }
   if (J.write_stats && c == 0 && tid == 0) {
@@ -200,8 +230,8 @@ __global__ void __launch_bounds__(kJBlock) k_jacobi(SimArgs a, JacobiArgs J) {
   }
 }
 
-size_t jacobi_smem_bytes(int rows_per_cta, int pitch) {
-  return (size_t)(3 * rows_per_cta + 4) * pitch * sizeof(float);
+size_t jacobi_smem_bytes(int rows_per_cta, int depth, int pitch) {
+  return (size_t)3 * (rows_per_cta + 2 * depth) * pitch * sizeof(float);
 }
 
 int jacobi_block() { return kJBlock; }
@@ -220,7 +250,7 @@ cudaError_t jacobi_max_ctas(size_t smem, int *per_sm) {
 }
 
 cudaError_t launch_jacobi(const SimArgs &a, const JacobiArgs &J, cudaStream_t st) {
-  const size_t sm = jacobi_smem_bytes(J.rows_per_cta, J.pitch);
+  const size_t sm = jacobi_smem_bytes(J.rows_per_cta, J.G > 1 ? J.depth : 1, J.pitch);
   if (J.G > 1) {
     cudaError_t e = cudaMemsetAsync(J.flags, 0, sizeof(unsigned) * (J.G + 1), st);
     if (e != cudaSuccess) return e;

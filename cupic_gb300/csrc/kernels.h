@@ -28,7 +28,7 @@ cudaError_t launch_load_scatter(const SimArgs &a, int sp, const float4 *tmp, int
 cudaError_t launch_pack_rows(const SimArgs &a, int sp, const int64_t *off, float4 *out32,
                              double *out64, cudaStream_t st);
 
-size_t jacobi_smem_bytes(int rows_per_cta, int pitch);
+size_t jacobi_smem_bytes(int rows_per_cta, int depth, int pitch);
 int jacobi_block();
 cudaError_t jacobi_set_smem(size_t bytes);
 cudaError_t jacobi_max_ctas(size_t smem, int *per_sm);

@@ -21,8 +21,6 @@ namespace cupic {
 
 namespace {
 
-constexpr int kPushBlock = 512;
-constexpr int kPushPPT = 2;
 constexpr int kInjBlock = 1024;
 constexpr unsigned kFull = 0xffffffffu;
 
@@ -166,121 +164,201 @@ __global__ void k_leapfrog_start(SimArgs a) {
 // ---------------------------------------------------------------------------
 // fused push + wrap + row binning + deposition, one block per cell row s
 // handling both species (particles.cu:110-231, cc.cu:303-810, mesh.cu:162-293)
+//
+// The row's particles stream through a ring of kStages shared-memory chunks
+// of CH = PB*PPT particles filled by 1-D bulk copies (TMA) that run
+// kStages-1 chunks ahead of the compute.  Thread t handles particles
+// j*PB + t (j < PPT) of a chunk; one block-wide scan per chunk gives every
+// stayer its slot (the stayers are compacted in place, keeping their order)
+// and every mover its slot in the staging buffer of its new row.  In-place
+// compaction is safe because no write goes past the chunk being processed
+// and every later chunk is disjoint from it.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kPushBlock) k_push_deposit(SimArgs a) {
-  extern __shared__ unsigned long long psm[];
-  constexpr int NW = kPushBlock / 32;
+namespace {
+constexpr int kPB = 512;       // threads
+constexpr int kPPT = 2;        // particles per thread per chunk
+constexpr int kStages = 4;     // chunks in flight
+constexpr int kCH = kPB * kPPT;
+}  // namespace
+
+size_t push_smem_bytes(int nnx) {
+  return (size_t)kStages * kCH * sizeof(float4) + (size_t)4 * nnx * sizeof(unsigned long long) +
+         (size_t)2 * nnx * sizeof(float2);
+}
+
+__global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
+  extern __shared__ __align__(128) unsigned char push_raw[];
+  constexpr int NW = kPB / 32;
+  constexpr int NE = kPPT * NW;  // scan entries per chunk, (j, warp) in j-major order
   const int s = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nnx = a.nnx;
-  unsigned long long *rtile = psm;                       // 4 node rows s-1..s+2
-  float2 *etile = reinterpret_cast<float2 *>(psm + 4 * nnx);  // node rows s, s+1
-  __shared__ uint32_t wsum[NW];
-  __shared__ uint32_t woff[NW];
-  __shared__ uint32_t wtot;
-  __shared__ unsigned long long s_abs, s_rem;
+  float4 *stage = reinterpret_cast<float4 *>(push_raw);
+  unsigned long long *rtile = reinterpret_cast<unsigned long long *>(stage + kStages * kCH);
+  float2 *etile = reinterpret_cast<float2 *>(rtile + 4 * nnx);
+  __shared__ __align__(8) uint64_t full[kStages];
+  __shared__ unsigned long long wsum[NE];
+  __shared__ unsigned long long woff[NE];
+  __shared__ unsigned long long wtot;
+  __shared__ unsigned long long s_cnt[4];
 
   Ctl *ctl = a.ctl;
+  const int n0 = a.sp[0].cnt[s], n1 = a.sp[1].cnt[s];
+  const int nc0 = (n0 + kCH - 1) / kCH, nct = nc0 + (n1 + kCH - 1) / kCH;
+  float4 *row0 = a.sp[0].parts + a.sp[0].seg[s];
+  float4 *row1 = a.sp[1].parts + a.sp[1].seg[s];
+
+  if (tid == 0) {
+    for (int i = 0; i < kStages; ++i) mbar_init(&full[i], 1);
+    fence_mbar_init();
+    for (int i = 0; i < 4; ++i) s_cnt[i] = 0ull;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    for (int k = 0; k < kStages && k < nct; ++k) {
+      const bool sp1 = k >= nc0;
+      const int q = sp1 ? k - nc0 : k;
+      const int nn = sp1 ? n1 : n0;
+      const int cnt = min(kCH, nn - q * kCH);
+      mbar_arrive_expect_tx(&full[k], (uint32_t)cnt * 16u);
+      bulk_g2s(stage + k * kCH, (sp1 ? row1 : row0) + (size_t)q * kCH, (uint32_t)cnt * 16u, &full[k]);
+    }
+  }
   RhoTile T{rtile, s - 1, 4, nnx, a.rho[ctl->cur ^ 1]};
-  for (int k = tid; k < 4 * nnx; k += kPushBlock) rtile[k] = 0ull;
-  for (int k = tid; k < 2 * nnx; k += kPushBlock) etile[k] = a.E[(size_t)s * nnx + k];
+  for (int k = tid; k < 4 * nnx; k += kPB) rtile[k] = 0ull;
+  for (int k = tid; k < 2 * nnx; k += kPB) etile[k] = a.E[(size_t)s * nnx + k];
   __syncthreads();
 
   uint32_t fl = 0;
+  unsigned nabs[2] = {0u, 0u}, nrem[2] = {0u, 0u};
   const uint32_t lt = (1u << lane) - 1u;
-  for (int sp = 0; sp < 2; ++sp) {
+  int c_stay = 0, c_up = 0, c_dn = 0;
+  for (int k = 0; k < nct; ++k) {
+    const int sp = k >= nc0 ? 1 : 0;
+    const int q = sp ? k - nc0 : k;
+    const int nn = sp ? n1 : n0;
     const SpeciesDev &S = a.sp[sp];
-    const int n = S.cnt[s];
-    float4 *row = S.parts + S.seg[s];
-    float4 *sup = S.stage_up + (size_t)s * S.stage_cap;
-    float4 *sdn = S.stage_down + (size_t)s * S.stage_cap;
+    float4 *row = sp ? row1 : row0;
+    if (k == nc0) {  // species boundary
+      c_stay = c_up = c_dn = 0;
+    }
+    const int st = k % kStages;
+    if (!mbar_wait(&full[st], (uint32_t)((k / kStages) & 1))) fl |= CUPIC_FLAG_TIMEOUT;
     const float dtqm = a.dtqm[sp];
-    const long long q = sp == 0 ? -1 : 1;
-    int c_stay = 0, c_up = 0, c_dn = 0;
-    unsigned nabs = 0, nrem = 0;
-    if (tid == 0) {
-      s_abs = 0ull;
-      s_rem = 0ull;
-    }
-    for (int base = 0; base < n; base += kPushBlock * kPushPPT) {
-      float4 pv[kPushPPT];
+    const int cnt = min(kCH, nn - q * kCH);
+    float4 p[kPPT];
+    int cat[kPPT];
 #pragma unroll
-      for (int j = 0; j < kPushPPT; ++j) {
-        const int idx = base + j * kPushBlock + tid;
-        if (idx < n) pv[j] = row[idx];
-      }
-#pragma unroll
-      for (int j = 0; j < kPushPPT; ++j) {
-        const int idx = base + j * kPushBlock + tid;
-        const bool valid = idx < n;
-        float4 p = pv[j];
-        int cat = 3;  // 0 stay, 1 up, 2 down, 3 none
-        if (valid) {
-          float ex, ey;
-          gather_tile(a, etile, p.x, p.y, s, ex, ey);
-          p.z = __fmaf_rn(dtqm, ex, p.z);
-          p.w = __fmaf_rn(dtqm, ey, p.w);
-          p.x = __fmaf_rn(a.dt, p.z, p.x);
-          p.y = __fmaf_rn(a.dt, p.w, p.y);
-          p.x = wrap_x(a, p.x);
-          const Cls c = classify(a, p, s);
-          fl |= c.flag;
-          if (c.dest == kRowAbsorbed) {
-            ++nabs;
-          } else if (c.dest == kRowRemoved) {
-            ++nrem;
-          } else {
-            cat = c.dest == s ? 0 : (c.dest == s + 1 ? 1 : 2);
-          }
+    for (int j = 0; j < kPPT; ++j) {
+      const int idx = j * kPB + tid;
+      cat[j] = 3;  // 0 stay, 1 up, 2 down, 3 none
+      if (idx < cnt) {
+        float4 v = stage[st * kCH + idx];
+        float ex, ey;
+        gather_tile(a, etile, v.x, v.y, s, ex, ey);
+        v.z = __fmaf_rn(dtqm, ex, v.z);
+        v.w = __fmaf_rn(dtqm, ey, v.w);
+        v.x = __fmaf_rn(a.dt, v.z, v.x);
+        v.y = __fmaf_rn(a.dt, v.w, v.y);
+        v.x = wrap_x(a, v.x);
+        const Cls c = classify(a, v, s);
+        fl |= c.flag;
+        if (c.dest == kRowAbsorbed) {
+          ++nabs[sp];
+        } else if (c.dest == kRowRemoved) {
+          ++nrem[sp];
+        } else {
+          cat[j] = c.dest == s ? 0 : (c.dest == s + 1 ? 1 : 2);
         }
-        const uint32_t bs = __ballot_sync(kFull, cat == 0);
-        const uint32_t bu = __ballot_sync(kFull, cat == 1);
-        const uint32_t bd = __ballot_sync(kFull, cat == 2);
-        if (lane == 0) wsum[warp] = __popc(bs) | (__popc(bu) << 10) | (__popc(bd) << 20);
-        __syncthreads();
-        if (warp == 0) {
-          const uint32_t v = lane < NW ? wsum[lane] : 0u;
-          uint32_t inc = v;
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t u = __shfl_up_sync(kFull, inc, o);
-            if (lane >= o) inc += u;
-          }
-          if (lane < NW) woff[lane] = inc - v;
-          if (lane == 31) wtot = inc;
-        }
-        __syncthreads();
-        const uint32_t off = woff[warp], tot = wtot;
-        if (cat == 0) {
-          const int pos = c_stay + (int)(off & 1023u) + __popc(bs & lt);
-          row[pos] = p;
-        } else if (cat == 1) {
-          const int pos = c_up + (int)((off >> 10) & 1023u) + __popc(bu & lt);
-          if (pos < S.stage_cap) sup[pos] = p; else fl |= CUPIC_FLAG_STAGE;
-        } else if (cat == 2) {
-          const int pos = c_dn + (int)((off >> 20) & 1023u) + __popc(bd & lt);
-          if (pos < S.stage_cap) sdn[pos] = p; else fl |= CUPIC_FLAG_STAGE;
-        }
-        if (cat < 3) T.deposit(a, p.x, p.y, q);
-        c_stay += (int)(tot & 1023u);
-        c_up += (int)((tot >> 10) & 1023u);
-        c_dn += (int)((tot >> 20) & 1023u);
-        __syncthreads();
+        p[j] = v;
       }
     }
-    const unsigned wa = __reduce_add_sync(kFull, nabs), wr = __reduce_add_sync(kFull, nrem);
-    if (lane == 0 && (wa | wr)) {
-      atomicAdd(&s_abs, (unsigned long long)wa);
-      atomicAdd(&s_rem, (unsigned long long)wr);
+    uint32_t bs[kPPT], bu[kPPT], bd[kPPT];
+#pragma unroll
+    for (int j = 0; j < kPPT; ++j) {
+      bs[j] = __ballot_sync(kFull, cat[j] == 0);
+      bu[j] = __ballot_sync(kFull, cat[j] == 1);
+      bd[j] = __ballot_sync(kFull, cat[j] == 2);
+      if (lane == 0)
+        wsum[j * NW + warp] = (unsigned long long)__popc(bs[j]) |
+                              ((unsigned long long)__popc(bu[j]) << 21) |
+                              ((unsigned long long)__popc(bd[j]) << 42);
     }
     __syncthreads();
-    if (tid == 0) {
+    // every thread holds its particles: refill this stage with chunk k+kStages
+    if (tid == 0 && k + kStages < nct) {
+      const int k2 = k + kStages;
+      const bool sp1 = k2 >= nc0;
+      const int q2 = sp1 ? k2 - nc0 : k2;
+      const int nn2 = sp1 ? n1 : n0;
+      const int cnt2 = min(kCH, nn2 - q2 * kCH);
+      mbar_arrive_expect_tx(&full[st], (uint32_t)cnt2 * 16u);
+      bulk_g2s(stage + st * kCH, (sp1 ? row1 : row0) + (size_t)q2 * kCH, (uint32_t)cnt2 * 16u,
+               &full[st]);
+    }
+    if (warp == 0) {
+      unsigned long long carry = 0ull;
+#pragma unroll
+      for (int b = 0; b < NE; b += 32) {
+        const unsigned long long v = (b + lane < NE) ? wsum[b + lane] : 0ull;
+        unsigned long long inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const unsigned long long u = __shfl_up_sync(kFull, inc, o);
+          if (lane >= o) inc += u;
+        }
+        if (b + lane < NE) woff[b + lane] = carry + inc - v;
+        carry += __shfl_sync(kFull, inc, 31);
+      }
+      if (lane == 0) wtot = carry;
+    }
+    __syncthreads();
+    float4 *sup = S.stage_up + (size_t)s * S.stage_cap;
+    float4 *sdn = S.stage_down + (size_t)s * S.stage_cap;
+    const long long qc = sp == 0 ? -1 : 1;
+#pragma unroll
+    for (int j = 0; j < kPPT; ++j) {
+      const unsigned long long off = woff[j * NW + warp];
+      if (cat[j] == 0) {
+        row[c_stay + (int)(off & 0x1fffffull) + __popc(bs[j] & lt)] = p[j];
+      } else if (cat[j] == 1) {
+        const int pos = c_up + (int)((off >> 21) & 0x1fffffull) + __popc(bu[j] & lt);
+        if (pos < S.stage_cap) sup[pos] = p[j]; else fl |= CUPIC_FLAG_STAGE;
+      } else if (cat[j] == 2) {
+        const int pos = c_dn + (int)((off >> 42) & 0x1fffffull) + __popc(bd[j] & lt);
+        if (pos < S.stage_cap) sdn[pos] = p[j]; else fl |= CUPIC_FLAG_STAGE;
+      }
+      if (cat[j] < 3) T.deposit(a, p[j].x, p[j].y, qc);
+    }
+    const unsigned long long tot = wtot;
+    c_stay += (int)(tot & 0x1fffffull);
+    c_up += (int)((tot >> 21) & 0x1fffffull);
+    c_dn += (int)((tot >> 42) & 0x1fffffull);
+    const bool last_of_species = (k == nct - 1) || (k == nc0 - 1);
+    if (tid == 0 && last_of_species) {
       S.nstay[s] = c_stay;
       S.nup[s] = min(c_up, S.stage_cap);
       S.ndown[s] = min(c_dn, S.stage_cap);
-      if (s_abs) atomicAdd(&ctl->absorbed[sp], s_abs);
-      if (s_rem) atomicAdd(&ctl->removed[sp], s_rem);
     }
-    __syncthreads();
+  }
+  for (int sp = 0; sp < 2; ++sp) {  // rows with no particles of a species
+    if ((sp == 0 && nc0 == 0) || (sp == 1 && nct == nc0)) {
+      if (tid == 0) {
+        a.sp[sp].nstay[s] = 0;
+        a.sp[sp].nup[s] = 0;
+        a.sp[sp].ndown[s] = 0;
+      }
+    }
+    const unsigned wa = __reduce_add_sync(kFull, nabs[sp]);
+    const unsigned wr = __reduce_add_sync(kFull, nrem[sp]);
+    if (lane == 0 && (wa | wr)) {
+      atomicAdd(&s_cnt[2 * sp], (unsigned long long)wa);
+      atomicAdd(&s_cnt[2 * sp + 1], (unsigned long long)wr);
+    }
+  }
+  __syncthreads();
+  if (tid < 2) {
+    if (s_cnt[2 * tid]) atomicAdd(&ctl->absorbed[tid], s_cnt[2 * tid]);
+    if (s_cnt[2 * tid + 1]) atomicAdd(&ctl->removed[tid], s_cnt[2 * tid + 1]);
   }
   flush_tile(T, a.nny);
   fl = __reduce_or_sync(kFull, fl);
@@ -316,48 +394,91 @@ __global__ void k_arrive(SimArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// injection of the half-Maxwellian flux at y = Ly (cc.cu:179-256), one block
-// per species.  Draw k of step i uses Philox counter {k, i_lo, i_hi, 1<<8|sp}.
+// injection of the half-Maxwellian flux at y = Ly (cc.cu:179-256), in three
+// kernels:
+//   k_inject_sched   the step's count and the injection time of every draw,
+//                    accumulated one dtin at a time as the reference does
+//   k_inject_gen     one thread per draw: Philox4x32-10 draw {k, i_lo, i_hi,
+//                    1<<8|sp}, Maxwellian/Rayleigh velocities, field at the
+//                    injection point, the partial-step push, classification
+//   k_inject_append  one block per species: stable rank of each draw within
+//                    its destination row, append, deposit
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kInjBlock) k_inject(SimArgs a) {
+__global__ void k_inject_sched(SimArgs a) {
+  const int sp = threadIdx.x;
+  if (sp > 1) return;
+  const SpeciesDev &S = a.sp[sp];
+  Ctl *ctl = a.ctl;
+  const double t = ctl->t;
+  const double fpt = t + a.dt_d;
+  if (!ctl->tin_set[sp]) {
+    ctl->tin[sp] = t + a.dtin[sp];
+    ctl->tin_set[sp] = 1;
+  }
+  double tin = ctl->tin[sp];
+  int in = 0;
+  if (tin < fpt) in = 1 + (int)((fpt - tin) / a.dtin[sp]);
+  const int ne = in < S.inj_cap ? in : S.inj_cap;
+  if (in > ne) atomicOr(&ctl->step_flags, (uint32_t)CUPIC_FLAG_CAPACITY);
+  for (int k = 0; k < in; ++k) {
+    if (k < ne) S.inj_tin[k] = tin;
+    tin += a.dtin[sp];
+  }
+  ctl->tin[sp] = tin;
+  ctl->inj_count[sp] = in;
+  ctl->inj_gen[sp] = ne;
+}
+
+__global__ void k_inject_gen(SimArgs a) {
+  const int sp = blockIdx.y;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const Ctl *ctl = a.ctl;
+  const int ne = ctl->inj_gen[sp];
+  if (k >= ne) return;
+  const SpeciesDev &S = a.sp[sp];
+  const double t = ctl->t, fpt = t + a.dt_d, fvt = t + 0.5 * a.dt_d;
+  const double sig = a.sig[sp], qm = a.qm[sp];
+  const int64_t step = ctl->step;
+  const size_t top = (size_t)(a.nny - 1) * a.nnx;
+  const uint4 r = philox4x32_10(make_uint4((uint32_t)k, (uint32_t)step, (uint32_t)((uint64_t)step >> 32),
+                                           (uint32_t)((kPurposeInject << 8) | sp)),
+                                a.k0, a.k1);
+  double x = u01(r.x) * a.Lx_d;
+  double sn, cs;
+  dev_sincos2pi(u01(r.z), &sn, &cs);
+  double vx = sig * (sqrt(-2.0 * dev_log(u01(r.y))) * cs);
+  double vy = -(sig * sqrt(-2.0 * dev_log(u01(r.w))));
+  const int ic = cfloord(x * a.inv_ds_d, 0, a.ncx - 1);
+  const double fx = clamp01d(x * a.inv_ds_d - (double)ic);
+  const float2 e0 = a.E[top + ic], e1 = a.E[top + ic + 1];
+  const double epx = (1.0 - fx) * (double)e0.x + fx * (double)e1.x;
+  const double epy = (1.0 - fx) * (double)e0.y + fx * (double)e1.y;
+  const double tin = S.inj_tin[k];
+  const double dp = fpt - tin, dv = fvt - tin;
+  x = x + dp * vx;
+  const double y = a.Ly_d + dp * vy;
+  vx = vx + dv * (qm * epx);
+  vy = vy + dv * (qm * epy);
+  float4 p = make_float4((float)x, (float)y, (float)vx, (float)vy);
+  p.x = wrap_x(a, p.x);
+  const Cls c = classify(a, p, -1);
+  if (c.flag) atomicOr(&a.ctl->step_flags, c.flag);
+  S.inj_p[k] = p;
+  S.inj_d[k] = c.dest;
+}
+
+__global__ void __launch_bounds__(kInjBlock) k_inject_append(SimArgs a) {
   extern __shared__ int running[];  // [ncy] injected per destination row
   constexpr int NW = kInjBlock / 32;
   const int sp = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const SpeciesDev &S = a.sp[sp];
   Ctl *ctl = a.ctl;
-  __shared__ int s_in;
-  __shared__ double s_t;
   __shared__ unsigned s_rem;
-  if (tid == 0) {
-    const double t = ctl->t;
-    const double fpt = t + a.dt_d;
-    if (!ctl->tin_set[sp]) {
-      ctl->tin[sp] = t + a.dtin[sp];
-      ctl->tin_set[sp] = 1;
-    }
-    double tin = ctl->tin[sp];
-    int in = 0;
-    if (tin < fpt) in = 1 + (int)((fpt - tin) / a.dtin[sp]);
-    const int ne = in < S.inj_cap ? in : S.inj_cap;
-    if (in > ne) atomicOr(&ctl->step_flags, (uint32_t)CUPIC_FLAG_CAPACITY);
-    for (int k = 0; k < in; ++k) {
-      if (k < ne) S.inj_tin[k] = tin;
-      tin += a.dtin[sp];
-    }
-    ctl->tin[sp] = tin;
-    ctl->inj_count[sp] = in;
-    s_in = ne;
-    s_t = t;
-    s_rem = 0;
-  }
+  if (tid == 0) s_rem = 0;
   for (int k = tid; k < a.ncy; k += kInjBlock) running[k] = 0;
   __syncthreads();
-  const int ne = s_in;
-  const double t = s_t, fpt = t + a.dt_d, fvt = t + 0.5 * a.dt_d;
-  const double sig = a.sig[sp], qm = a.qm[sp];
+  const int ne = ctl->inj_gen[sp];
   const long long q = sp == 0 ? -1 : 1;
-  const int64_t step = ctl->step;
-  const size_t top = (size_t)(a.nny - 1) * a.nnx;
   unsigned long long *rho_next = a.rho[ctl->cur ^ 1];
   uint32_t fl = 0;
   unsigned nrem = 0;
@@ -366,31 +487,8 @@ __global__ void __launch_bounds__(kInjBlock) k_inject(SimArgs a) {
     int d = kRowRemoved;
     float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
     if (k < ne) {
-      const uint4 r = philox4x32_10(
-          make_uint4((uint32_t)k, (uint32_t)step, (uint32_t)((uint64_t)step >> 32),
-                     (uint32_t)((kPurposeInject << 8) | sp)),
-          a.k0, a.k1);
-      double x = u01(r.x) * a.Lx_d;
-      double sn, cs;
-      dev_sincos2pi(u01(r.z), &sn, &cs);
-      double vx = sig * (sqrt(-2.0 * dev_log(u01(r.y))) * cs);
-      double vy = -(sig * sqrt(-2.0 * dev_log(u01(r.w))));
-      const int ic = cfloord(x * a.inv_ds_d, 0, a.ncx - 1);
-      const double fx = clamp01d(x * a.inv_ds_d - (double)ic);
-      const float2 e0 = a.E[top + ic], e1 = a.E[top + ic + 1];
-      const double epx = (1.0 - fx) * (double)e0.x + fx * (double)e1.x;
-      const double epy = (1.0 - fx) * (double)e0.y + fx * (double)e1.y;
-      const double tin = S.inj_tin[k];
-      const double dp = fpt - tin, dv = fvt - tin;
-      x = x + dp * vx;
-      const double y = a.Ly_d + dp * vy;
-      vx = vx + dv * (qm * epx);
-      vy = vy + dv * (qm * epy);
-      p = make_float4((float)x, (float)y, (float)vx, (float)vy);
-      p.x = wrap_x(a, p.x);
-      const Cls c = classify(a, p, -1);
-      fl |= c.flag;
-      d = c.dest;
+      p = S.inj_p[k];
+      d = S.inj_d[k];
       if (d < 0) ++nrem;
     }
     // stable rank of each draw within its destination row, in draw order
@@ -496,10 +594,6 @@ cudaError_t launch_leapfrog_start(const SimArgs &a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-size_t push_smem_bytes(int nnx) {
-  return (size_t)4 * nnx * sizeof(unsigned long long) + (size_t)2 * nnx * sizeof(float2);
-}
-
 // the attribute only grows, so contexts of different sizes can coexist
 cudaError_t push_set_smem(size_t bytes) {
   static size_t cur = 48 * 1024;
@@ -512,7 +606,7 @@ cudaError_t push_set_smem(size_t bytes) {
 
 cudaError_t launch_push_deposit(const SimArgs &a, cudaStream_t st) {
   const size_t sm = push_smem_bytes(a.nnx);
-  k_push_deposit<<<a.ncy, kPushBlock, sm, st>>>(a);
+  k_push_deposit<<<a.ncy, kPB, sm, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -522,7 +616,14 @@ cudaError_t launch_arrive(const SimArgs &a, cudaStream_t st) {
 }
 
 cudaError_t launch_inject(const SimArgs &a, cudaStream_t st) {
-  k_inject<<<2, kInjBlock, a.ncy * sizeof(int), st>>>(a);
+  const int cap = max(a.sp[0].inj_cap, a.sp[1].inj_cap);
+  k_inject_sched<<<1, 32, 0, st>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_inject_gen<<<dim3((cap + 127) / 128, 2), 128, 0, st>>>(a);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_inject_append<<<2, kInjBlock, a.ncy * sizeof(int), st>>>(a);
   return cudaGetLastError();
 }
 

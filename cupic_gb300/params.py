@@ -100,6 +100,7 @@ def workload_params(name="small", **over):
         p.mi, p.kti = 1836.0, 0.1
         p.tol, p.min_sweeps, p.max_sweeps = 0.0, 200, 200
         p.init_tol, p.init_min_sweeps, p.init_max_sweeps = 0.0, 200, 200
+        p.check_every = 200  # fixed sweep count: only the last sweep's residual is reported
         p.seed = 1
     elif name == "tiny":
         p.ncx, p.ncy = 16, 32
