@@ -181,7 +181,7 @@ int plan_jacobi(cupic_ctx *c) {
   const int M = c->a.nny - 2, nnx = c->a.nnx;
   int dev_max = 0;
   CU(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
-  const int P = nnx;
+  const int P = (nnx + 3) / 4 * 4;  // 16-byte aligned rows
   const size_t avail = (size_t)dev_max - 1024;  // static shared memory of the kernel
   const long long rows_fit = (long long)(avail / (3 * sizeof(float) * (size_t)P));
   const char *env = getenv("CUPIC_JACOBI_CTAS");
@@ -233,6 +233,8 @@ JacobiArgs jargs(const cupic_ctx *c, double tol, int mn, int mx, int chk, int fi
   J.rows_per_cta = c->jB;
   J.depth = c->jK;
   J.pitch = c->jP;
+  J.vec = ((c->a.nnx - 1) % 4 == 0) ? 1 : 0;
+  if (getenv("CUPIC_JACOBI_SCALAR")) J.vec = 0;
   J.do_field = field;
   J.write_stats = 1;
   J.flags = c->jflags;

@@ -84,7 +84,8 @@ struct JacobiArgs {
   int32_t G;              // CTAs (cooperative)
   int32_t rows_per_cta;   // most interior rows owned by one CTA: ceil((nny-2)/G)
   int32_t depth;          // temporal blocking: sweeps between halo exchanges (G > 1)
-  int32_t pitch;          // smem row pitch in floats
+  int32_t pitch;          // smem row pitch in floats (a multiple of 4)
+  int32_t vec;            // 1: (nnx-1) % 4 == 0, sweep 4 nodes per thread with float4
   int32_t do_field;       // 1: derive E after the last sweep
   int32_t write_stats;    // 1: store sweeps/residual in the control block
   unsigned int *flags;    // [G] last sweep published by each CTA
@@ -232,6 +233,32 @@ __device__ __forceinline__ void gather_tile(const SimArgs &a, const float2 *tile
   ey = __fmaf_rn(w10, e10.y, ey);
   ey = __fmaf_rn(w01, e01.y, ey);
   ey = __fmaf_rn(w11, e11.y, ey);
+  Epx = ex;
+  Epy = ey;
+}
+
+// CIC field from a shared tile of node pairs: tile4[r*ncx + i] =
+// {Ex(i), Ey(i), Ex(i+1), Ey(i+1)} of node row s+r, so a particle's four
+// nodes come in two 16-byte loads.  Same operations, in the same order, as
+// gather_tile.
+__device__ __forceinline__ void gather_tile4(const SimArgs &a, const float4 *tile4, float x, float y,
+                                             int s, float &Epx, float &Epy) {
+  const float sx = __fmul_rn(x, a.inv_ds);
+  const int ic = cfloorf(sx, 0, a.ncx - 1);
+  const float fx = clamp01f(__fsub_rn(sx, (float)ic));
+  const float fy = clamp01f(__fsub_rn(__fmul_rn(y, a.inv_ds), (float)s));
+  const float gx = __fsub_rn(1.0f, fx), gy = __fsub_rn(1.0f, fy);
+  const float w00 = __fmul_rn(gx, gy), w10 = __fmul_rn(fx, gy);
+  const float w01 = __fmul_rn(gx, fy), w11 = __fmul_rn(fx, fy);
+  const float4 lo = tile4[ic], hi = tile4[a.ncx + ic];
+  float ex = __fmul_rn(w00, lo.x);
+  ex = __fmaf_rn(w10, lo.z, ex);
+  ex = __fmaf_rn(w01, hi.x, ex);
+  ex = __fmaf_rn(w11, hi.z, ex);
+  float ey = __fmul_rn(w00, lo.y);
+  ey = __fmaf_rn(w10, lo.w, ey);
+  ey = __fmaf_rn(w01, hi.y, ey);
+  ey = __fmaf_rn(w11, hi.w, ey);
   Epx = ex;
   Epy = ey;
 }

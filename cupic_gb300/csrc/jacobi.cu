@@ -105,6 +105,15 @@ __global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) 
   __syncthreads();
 
   const int W = nnx - 1;  // computed columns 0 .. nnx-2; column nnx-1 mirrors 0
+  // thread -> (column group gx, row offset gy), fixed for the whole solve.
+  // Vector path: a group is 4 consecutive nodes (float4); scalar path: 1.
+  const bool vec = J.vec != 0;
+  const int NG = vec ? (W >> 2) : W;           // column groups per row
+  const int TPR = min(NG, kJBlock);            // threads per row
+  const int RPI = kJBlock / TPR;               // rows per iteration
+  const int gx = tid % TPR, gy = tid / TPR;
+  const int lane = tid & 31;
+  const int iters_c = (NG + TPR - 1) / TPR;
   int src = 0, done = 0, nchk = 0;
   float last = INFINITY;
   for (int s = 1; s <= J.max_sweeps; ++s) {
@@ -116,21 +125,59 @@ __global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) 
     const int u1 = min(nny - 2, r1 - 1 + K - m) + 1 - lo;
     const int o0 = r0 - lo, o1 = r1 - lo;            // owned local rows
     float md = 0.0f;
-    const int nu = (u1 - u0) * W;
-    for (int k = tid; k < nu; k += kJBlock) {
-      const int lr = k / W + u0, i = k - (lr - u0) * W;
+    const int iters_r = (u1 - u0 + RPI - 1) / RPI;
+    for (int ir = 0; ir < iters_r; ++ir) {
+      const int lr = u0 + gy + ir * RPI;
+      const bool rowok = gy < RPI && lr < u1;
+      const bool own = check && rowok && lr >= o0 && lr < o1;
       const float *cr = S + lr * P;
-      const float wv = (i == 0) ? cr[W - 1] : cr[i - 1];
-      const float v = __fmul_rn(
-          0.25f,
-          __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(bsrc[lr * P + i], wv), cr[i + 1]), cr[P + i]),
-                    cr[i - P]));
-      D[lr * P + i] = v;
-      const bool own = check && lr >= o0 && lr < o1;
-      if (own) md = fmaxf(md, fabsf(__fsub_rn(v, cr[i])));
-      if (i == 0) {
-        D[lr * P + W] = v;
-        if (own) md = fmaxf(md, fabsf(__fsub_rn(v, cr[W])));
+      for (int ic = 0; ic < iters_c; ++ic) {
+        const int cg = gx + ic * TPR;
+        const bool ok = rowok && cg < NG;
+        if (vec) {
+          const int col = cg << 2;
+          float4 c4 = make_float4(0.f, 0.f, 0.f, 0.f), n4 = c4, s4 = c4, b4 = c4;
+          if (ok) {
+            c4 = *reinterpret_cast<const float4 *>(cr + col);
+            n4 = *reinterpret_cast<const float4 *>(cr + P + col);
+            s4 = *reinterpret_cast<const float4 *>(cr - P + col);
+            b4 = *reinterpret_cast<const float4 *>(bsrc + lr * P + col);
+          }
+          float lf = __shfl_up_sync(0xffffffffu, c4.w, 1);
+          float rt = __shfl_down_sync(0xffffffffu, c4.x, 1);
+          if (ok) {
+            // neighbours not held by the adjacent lane come from shared memory;
+            // west of node 0 is node nnx-2, east of node nnx-2 is the seam copy
+            if (lane == 0 || gx == 0) lf = cg == 0 ? cr[W - 1] : cr[col - 1];
+            if (lane == 31 || gx == TPR - 1 || cg == NG - 1) rt = cr[col + 4];
+            float4 v;
+            v.x = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.x, lf), c4.y), n4.x), s4.x));
+            v.y = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.y, c4.x), c4.z), n4.y), s4.y));
+            v.z = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.z, c4.y), c4.w), n4.z), s4.z));
+            v.w = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.w, c4.z), rt), n4.w), s4.w));
+            *reinterpret_cast<float4 *>(D + lr * P + col) = v;
+            if (cg == 0) D[lr * P + W] = v.x;
+            if (own) {
+              md = fmaxf(md, fabsf(__fsub_rn(v.x, c4.x)));
+              md = fmaxf(md, fabsf(__fsub_rn(v.y, c4.y)));
+              md = fmaxf(md, fabsf(__fsub_rn(v.z, c4.z)));
+              md = fmaxf(md, fabsf(__fsub_rn(v.w, c4.w)));
+              if (cg == 0) md = fmaxf(md, fabsf(__fsub_rn(v.x, cr[W])));
+            }
+          }
+        } else if (ok) {
+          const int i = cg;
+          const float wv = (i == 0) ? cr[W - 1] : cr[i - 1];
+          const float v = __fmul_rn(
+              0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(bsrc[lr * P + i], wv), cr[i + 1]), cr[P + i]),
+                               cr[i - P]));
+          D[lr * P + i] = v;
+          if (own) md = fmaxf(md, fabsf(__fsub_rn(v, cr[i])));
+          if (i == 0) {
+            D[lr * P + W] = v;
+            if (own) md = fmaxf(md, fabsf(__fsub_rn(v, cr[W])));
+          }
+        }
       }
     }
     __syncthreads();

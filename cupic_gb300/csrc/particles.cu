@@ -28,36 +28,67 @@ __device__ __forceinline__ void raise_flags(Ctl *ctl, uint32_t f) {
   if (f) atomicOr(&ctl->step_flags, f);
 }
 
-// shared tile of node rows [row0, row0+nrows) of the charge accumulator;
-// deposits that fall outside go straight to global memory
+// Shared tile of node rows [row0, row0+nrows) of the charge accumulator.
+// Shared-memory atomics are native for 32-bit integers only, so each
+// fixed-point weight W (< = 2^32) is added as two exact halves, W >> 16 into
+// hi and W & 0xffff into lo.  Both halves of up to kFoldParticles particles
+// fit in an int32, so fold() moves them into the int64 tile t64 at least
+// that often; flush() adds t64 to global memory once.  Deposits that fall
+// outside the tile go straight to global memory as int64 atomics.
+constexpr int kFoldParticles = 16384;
+
 struct RhoTile {
-  unsigned long long *t;
+  int *hi, *lo;
+  long long *t64;
   int row0, nrows, nnx;
   unsigned long long *g;
 
-  __device__ __forceinline__ void add(int node_row, int i, long long v) const {
+  __device__ __forceinline__ void add(int node_row, int i, long long w, int q) const {
     const int tr = node_row - row0;
     if (tr >= 0 && tr < nrows) {
-      atomicAdd(&t[tr * nnx + i], (unsigned long long)v);
+      const int k = tr * nnx + i;
+      const int h = (int)(w >> 16), l = (int)(w & 0xffff);
+      atomicAdd(&hi[k], q * h);
+      atomicAdd(&lo[k], q * l);
     } else {
-      atomicAdd(&g[(size_t)node_row * nnx + i], (unsigned long long)v);
+      atomicAdd(&g[(size_t)node_row * nnx + i], (unsigned long long)(q * w));
     }
   }
-  __device__ __forceinline__ void deposit(const SimArgs &a, float x, float y, long long q) const {
+  __device__ __forceinline__ void deposit(const SimArgs &a, float x, float y, int q) const {
     const CicFixed c = cic_fixed(a, x, y);
-    add(c.jc, c.ic, q * c.w00);
-    add(c.jc, c.ic + 1, q * c.w10);
-    add(c.jc + 1, c.ic, q * c.w01);
-    add(c.jc + 1, c.ic + 1, q * c.w11);
+    add(c.jc, c.ic, c.w00, q);
+    add(c.jc, c.ic + 1, c.w10, q);
+    add(c.jc + 1, c.ic, c.w01, q);
+    add(c.jc + 1, c.ic + 1, c.w11, q);
+  }
+  // all threads; callers bracket it with __syncthreads()
+  __device__ __forceinline__ void zero() const {
+    for (int k = threadIdx.x; k < nrows * nnx; k += blockDim.x) {
+      hi[k] = 0;
+      lo[k] = 0;
+      t64[k] = 0;
+    }
+  }
+  __device__ __forceinline__ void fold() const {
+    for (int k = threadIdx.x; k < nrows * nnx; k += blockDim.x) {
+      t64[k] += (long long)hi[k] * 65536 + (long long)lo[k];
+      hi[k] = 0;
+      lo[k] = 0;
+    }
+  }
+  // fold + add to global memory; callers __syncthreads() before
+  __device__ __forceinline__ void flush(int nny) const {
+    for (int k = threadIdx.x; k < nrows * nnx; k += blockDim.x) {
+      const long long v = t64[k] + (long long)hi[k] * 65536 + (long long)lo[k];
+      const int r = row0 + k / nnx;
+      if (v != 0 && r >= 0 && r < nny)
+        atomicAdd(&g[(size_t)r * nnx + (k % nnx)], (unsigned long long)v);
+    }
   }
 };
 
-__device__ __forceinline__ void flush_tile(const RhoTile &T, int nny) {
-  for (int k = threadIdx.x; k < T.nrows * T.nnx; k += blockDim.x) {
-    const int r = T.row0 + k / T.nnx;
-    const unsigned long long v = T.t[k];
-    if (v != 0ull && r >= 0 && r < nny) atomicAdd(&T.g[(size_t)r * T.nnx + (k % T.nnx)], v);
-  }
+__host__ __device__ constexpr size_t rho_tile_bytes(int nrows, int nnx) {
+  return (size_t)nrows * nnx * (2 * sizeof(int) + sizeof(long long));
 }
 
 // classification of a pushed particle listed in row s (s < 0: injected)
@@ -109,23 +140,35 @@ __global__ void k_init_particles(SimArgs a) {
 // (mesh.cu:162-293; int64 fixed point, so the sum is order independent)
 // ---------------------------------------------------------------------------
 __global__ void k_deposit(SimArgs a) {
-  extern __shared__ unsigned long long dtile[];
-  const int s = blockIdx.x;
-  RhoTile T{dtile, s, 2, a.nnx, a.rho[a.ctl->cur]};
-  for (int k = threadIdx.x; k < 2 * a.nnx; k += blockDim.x) dtile[k] = 0ull;
+  extern __shared__ long long dtile[];
+  const int s = blockIdx.x, nnx = a.nnx;
+  RhoTile T{reinterpret_cast<int *>(dtile + 2 * nnx), reinterpret_cast<int *>(dtile + 2 * nnx) + 2 * nnx,
+            dtile, s, 2, nnx, a.rho[a.ctl->cur]};
+  T.zero();
   __syncthreads();
+  int since = 0;
   for (int sp = 0; sp < 2; ++sp) {
     const SpeciesDev &S = a.sp[sp];
     const float4 *row = S.parts + S.seg[s];
     const int n = S.cnt[s];
-    const long long q = sp == 0 ? -1 : 1;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-      const float4 p = row[k];
-      T.deposit(a, p.x, p.y, q);
+    const int q = sp == 0 ? -1 : 1;
+    for (int base = 0; base < n; base += blockDim.x) {
+      const int k = base + threadIdx.x;
+      if (k < n) {
+        const float4 p = row[k];
+        T.deposit(a, p.x, p.y, q);
+      }
+      since += blockDim.x;
+      if (since >= kFoldParticles) {  // block-uniform
+        __syncthreads();
+        T.fold();
+        __syncthreads();
+        since = 0;
+      }
     }
   }
   __syncthreads();
-  flush_tile(T, a.nny);
+  T.flush(a.nny);
 }
 
 // zero the accumulator the next deposit writes (rho[cur^1])
@@ -177,13 +220,13 @@ __global__ void k_leapfrog_start(SimArgs a) {
 namespace {
 constexpr int kPB = 512;       // threads
 constexpr int kPPT = 2;        // particles per thread per chunk
-constexpr int kStages = 4;     // chunks in flight
+constexpr int kStages = 3;     // chunks in flight
 constexpr int kCH = kPB * kPPT;
 }  // namespace
 
 size_t push_smem_bytes(int nnx) {
-  return (size_t)kStages * kCH * sizeof(float4) + (size_t)4 * nnx * sizeof(unsigned long long) +
-         (size_t)2 * nnx * sizeof(float2);
+  return (size_t)kStages * kCH * sizeof(float4) + rho_tile_bytes(4, nnx) +
+         (size_t)2 * (nnx - 1) * sizeof(float4);
 }
 
 __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
@@ -192,9 +235,12 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
   constexpr int NE = kPPT * NW;  // scan entries per chunk, (j, warp) in j-major order
   const int s = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nnx = a.nnx;
+  const int ncx = a.ncx;
   float4 *stage = reinterpret_cast<float4 *>(push_raw);
-  unsigned long long *rtile = reinterpret_cast<unsigned long long *>(stage + kStages * kCH);
-  float2 *etile = reinterpret_cast<float2 *>(rtile + 4 * nnx);
+  float4 *etile = stage + kStages * kCH;                        // 2*ncx node pairs
+  long long *t64 = reinterpret_cast<long long *>(etile + 2 * ncx);  // 4 node rows s-1..s+2
+  int *thi = reinterpret_cast<int *>(t64 + 4 * nnx);
+  int *tlo = thi + 4 * nnx;
   __shared__ __align__(8) uint64_t full[kStages];
   __shared__ unsigned long long wsum[NE];
   __shared__ unsigned long long woff[NE];
@@ -223,9 +269,13 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
       bulk_g2s(stage + k * kCH, (sp1 ? row1 : row0) + (size_t)q * kCH, (uint32_t)cnt * 16u, &full[k]);
     }
   }
-  RhoTile T{rtile, s - 1, 4, nnx, a.rho[ctl->cur ^ 1]};
-  for (int k = tid; k < 4 * nnx; k += kPB) rtile[k] = 0ull;
-  for (int k = tid; k < 2 * nnx; k += kPB) etile[k] = a.E[(size_t)s * nnx + k];
+  RhoTile T{thi, tlo, t64, s - 1, 4, nnx, a.rho[ctl->cur ^ 1]};
+  T.zero();
+  for (int k = tid; k < 2 * ncx; k += kPB) {
+    const int r = k / ncx, i = k - r * ncx;
+    const float2 e0 = a.E[(size_t)(s + r) * nnx + i], e1 = a.E[(size_t)(s + r) * nnx + i + 1];
+    etile[k] = make_float4(e0.x, e0.y, e1.x, e1.y);
+  }
   __syncthreads();
 
   uint32_t fl = 0;
@@ -254,7 +304,7 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
       if (idx < cnt) {
         float4 v = stage[st * kCH + idx];
         float ex, ey;
-        gather_tile(a, etile, v.x, v.y, s, ex, ey);
+        gather_tile4(a, etile, v.x, v.y, s, ex, ey);
         v.z = __fmaf_rn(dtqm, ex, v.z);
         v.w = __fmaf_rn(dtqm, ey, v.w);
         v.x = __fmaf_rn(a.dt, v.z, v.x);
@@ -314,7 +364,7 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
     __syncthreads();
     float4 *sup = S.stage_up + (size_t)s * S.stage_cap;
     float4 *sdn = S.stage_down + (size_t)s * S.stage_cap;
-    const long long qc = sp == 0 ? -1 : 1;
+    const int qc = sp == 0 ? -1 : 1;
 #pragma unroll
     for (int j = 0; j < kPPT; ++j) {
       const unsigned long long off = woff[j * NW + warp];
@@ -339,6 +389,10 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
       S.nup[s] = min(c_up, S.stage_cap);
       S.ndown[s] = min(c_dn, S.stage_cap);
     }
+    if ((k + 1) % (kFoldParticles / kCH) == 0 && k + 1 < nct) {  // block-uniform
+      __syncthreads();
+      T.fold();
+    }
   }
   for (int sp = 0; sp < 2; ++sp) {  // rows with no particles of a species
     if ((sp == 0 && nc0 == 0) || (sp == 1 && nct == nc0)) {
@@ -360,7 +414,7 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
     if (s_cnt[2 * tid]) atomicAdd(&ctl->absorbed[tid], s_cnt[2 * tid]);
     if (s_cnt[2 * tid + 1]) atomicAdd(&ctl->removed[tid], s_cnt[2 * tid + 1]);
   }
-  flush_tile(T, a.nny);
+  T.flush(a.nny);
   fl = __reduce_or_sync(kFull, fl);
   if (lane == 0) raise_flags(ctl, fl);
 }
@@ -577,7 +631,7 @@ cudaError_t launch_init_particles(const SimArgs &a, cudaStream_t st) {
 }
 
 cudaError_t launch_deposit(const SimArgs &a, cudaStream_t st) {
-  k_deposit<<<a.ncy, 256, 2 * a.nnx * sizeof(unsigned long long), st>>>(a);
+  k_deposit<<<a.ncy, 256, rho_tile_bytes(2, a.nnx), st>>>(a);
   return cudaGetLastError();
 }
 
