@@ -100,12 +100,11 @@ struct JacobiArgs {
 __device__ __forceinline__ float clamp01f(float v) { return fminf(fmaxf(v, 0.0f), 1.0f); }
 __device__ __forceinline__ double clamp01d(double v) { return fmin(fmax(v, 0.0), 1.0); }
 
-// floor(v) clamped to [lo, hi]; NaN -> lo
+// floor(v) clamped to [0, hi]; NaN -> 0.  cvt.rmi saturates out-of-range
+// values and maps NaN to 0, so one conversion and an integer clamp give the
+// same result as the oracle's explicit tests.
 __device__ __forceinline__ int cfloorf(float v, int lo, int hi) {
-  if (!(v >= (float)lo)) return lo;
-  if (v >= (float)(hi + 1)) return hi;
-  int i = (int)floorf(v);
-  return i > hi ? hi : i;
+  return min(max(__float2int_rd(v), lo), hi);
 }
 __device__ __forceinline__ int cfloord(double v, int lo, int hi) {
   if (!(v >= (double)lo)) return lo;
@@ -266,6 +265,7 @@ __device__ __forceinline__ void gather_tile4(const SimArgs &a, const float4 *til
 // fixed-point CIC weights (16 fractional bits per axis, 2^32 per particle)
 struct CicFixed {
   int ic, jc;
+  int FX, FY;  // offsets in the cell, 16 fractional bits, in [0, 65536]
   long long w00, w10, w01, w11;
 };
 
@@ -277,8 +277,9 @@ __device__ __forceinline__ CicFixed cic_fixed(const SimArgs &a, float x, float y
   const float sy = __fmul_rn(y, a.inv_ds);
   r.jc = cfloorf(sy, 0, a.ncy - 1);
   const float fy = clamp01f(__fsub_rn(sy, (float)r.jc));
-  const long long FX = __float2int_rn(__fmul_rn(fx, 65536.0f));
-  const long long FY = __float2int_rn(__fmul_rn(fy, 65536.0f));
+  r.FX = __float2int_rn(__fmul_rn(fx, 65536.0f));
+  r.FY = __float2int_rn(__fmul_rn(fy, 65536.0f));
+  const long long FX = r.FX, FY = r.FY;
   const long long GX = 65536 - FX, GY = 65536 - FY;
   r.w00 = GX * GY;
   r.w10 = FX * GY;

@@ -28,67 +28,98 @@ __device__ __forceinline__ void raise_flags(Ctl *ctl, uint32_t f) {
   if (f) atomicOr(&ctl->step_flags, f);
 }
 
-// Shared tile of node rows [row0, row0+nrows) of the charge accumulator.
-// Shared-memory atomics are native for 32-bit integers only, so each
-// fixed-point weight W (< = 2^32) is added as two exact halves, W >> 16 into
-// hi and W & 0xffff into lo.  Both halves of up to kFoldParticles particles
-// fit in an int32, so fold() moves them into the int64 tile t64 at least
-// that often; flush() adds t64 to global memory once.  Deposits that fall
-// outside the tile go straight to global memory as int64 atomics.
+// Charge deposition into shared memory by cell moments.  For the particles
+// of a cell, with 16-bit fixed-point offsets FX, FY in [0, 65536] and
+// GX = 65536-FX, GY = 65536-FY, the four node sums of q*weight follow exactly
+// from four integer moments of the cell:
+//   sum q GX GY = 65536^2 M1 - 65536 (MX + MY) + MXY      (lower-left node)
+//   sum q FX GY = 65536 MX - MXY                          (lower-right)
+//   sum q GX FY = 65536 MY - MXY                          (upper-left)
+//   sum q FX FY = MXY                                     (upper-right)
+// with M1 = sum q, MX = sum q FX, MY = sum q FY, MXY = sum q FX FY.  Shared
+// memory atomics are native for 32-bit integers only, so a particle adds q,
+// q FX, q FY and the two 16-bit halves of q FX FY to five int32 moment
+// planes; within kFoldParticles particles none of them can overflow, and
+// fold() turns the moments into int64 node sums that often.  flush() adds
+// the node sums to global memory once.  Deposits whose cell row is outside
+// the tile go straight to global memory as int64 node weights.
 constexpr int kFoldParticles = 16384;
 
-struct RhoTile {
-  int *hi, *lo;
-  long long *t64;
-  int row0, nrows, nnx;
+struct RhoMoments {
+  int *m;          // [5][ncr*ncx]: M1, MX, MY, MXY>>16 part, MXY low 16 bits
+  long long *node; // [(ncr+1)*nnx] node sums of this block
+  int crow0, ncr, ncx, nnx;
   unsigned long long *g;
 
-  __device__ __forceinline__ void add(int node_row, int i, long long w, int q) const {
-    const int tr = node_row - row0;
-    if (tr >= 0 && tr < nrows) {
-      const int k = tr * nnx + i;
-      const int h = (int)(w >> 16), l = (int)(w & 0xffff);
-      atomicAdd(&hi[k], q * h);
-      atomicAdd(&lo[k], q * l);
-    } else {
-      atomicAdd(&g[(size_t)node_row * nnx + i], (unsigned long long)(q * w));
-    }
-  }
   __device__ __forceinline__ void deposit(const SimArgs &a, float x, float y, int q) const {
     const CicFixed c = cic_fixed(a, x, y);
-    add(c.jc, c.ic, c.w00, q);
-    add(c.jc, c.ic + 1, c.w10, q);
-    add(c.jc + 1, c.ic, c.w01, q);
-    add(c.jc + 1, c.ic + 1, c.w11, q);
+    const int tr = c.jc - crow0;
+    if (tr >= 0 && tr < ncr) {
+      const int k = tr * ncx + c.ic, pl = ncr * ncx;
+      const unsigned long long fxy = (unsigned long long)c.FX * (unsigned long long)c.FY;
+      atomicAdd(&m[k], q);
+      atomicAdd(&m[pl + k], q * c.FX);
+      atomicAdd(&m[2 * pl + k], q * c.FY);
+      atomicAdd(&m[3 * pl + k], q * (int)(fxy >> 16));
+      atomicAdd(&m[4 * pl + k], q * (int)(fxy & 0xffffull));
+    } else {
+      const size_t n00 = (size_t)c.jc * nnx + c.ic;
+      atomicAdd(&g[n00], (unsigned long long)(q * c.w00));
+      atomicAdd(&g[n00 + 1], (unsigned long long)(q * c.w10));
+      atomicAdd(&g[n00 + nnx], (unsigned long long)(q * c.w01));
+      atomicAdd(&g[n00 + nnx + 1], (unsigned long long)(q * c.w11));
+    }
   }
-  // all threads; callers bracket it with __syncthreads()
   __device__ __forceinline__ void zero() const {
-    for (int k = threadIdx.x; k < nrows * nnx; k += blockDim.x) {
-      hi[k] = 0;
-      lo[k] = 0;
-      t64[k] = 0;
-    }
+    for (int k = threadIdx.x; k < 5 * ncr * ncx; k += blockDim.x) m[k] = 0;
+    for (int k = threadIdx.x; k < (ncr + 1) * nnx; k += blockDim.x) node[k] = 0;
   }
+  // moments -> node sums, then clear the moments; callers __syncthreads()
+  // before, and before the next deposit
   __device__ __forceinline__ void fold() const {
-    for (int k = threadIdx.x; k < nrows * nnx; k += blockDim.x) {
-      t64[k] += (long long)hi[k] * 65536 + (long long)lo[k];
-      hi[k] = 0;
-      lo[k] = 0;
+    const int pl = ncr * ncx;
+    for (int k = threadIdx.x; k < (ncr + 1) * nnx; k += blockDim.x) {
+      const int j = k / nnx, i = k - j * nnx;
+      long long v = 0;
+      if (i < ncx && j < ncr) {  // this node is the lower-left corner of cell (i, j)
+        const int c = j * ncx + i;
+        const long long mxy = (long long)m[3 * pl + c] * 65536 + m[4 * pl + c];
+        v += (long long)m[c] * 4294967296ll - 65536ll * ((long long)m[pl + c] + m[2 * pl + c]) + mxy;
+      }
+      if (i >= 1 && j < ncr) {  // lower-right corner of cell (i-1, j)
+        const int c = j * ncx + i - 1;
+        const long long mxy = (long long)m[3 * pl + c] * 65536 + m[4 * pl + c];
+        v += 65536ll * m[pl + c] - mxy;
+      }
+      if (i < ncx && j >= 1) {  // upper-left corner of cell (i, j-1)
+        const int c = (j - 1) * ncx + i;
+        const long long mxy = (long long)m[3 * pl + c] * 65536 + m[4 * pl + c];
+        v += 65536ll * m[2 * pl + c] - mxy;
+      }
+      if (i >= 1 && j >= 1) {  // upper-right corner of cell (i-1, j-1)
+        const int c = (j - 1) * ncx + i - 1;
+        v += (long long)m[3 * pl + c] * 65536 + m[4 * pl + c];
+      }
+      node[k] += v;
     }
+    __syncthreads();
+    for (int k = threadIdx.x; k < 5 * pl; k += blockDim.x) m[k] = 0;
   }
-  // fold + add to global memory; callers __syncthreads() before
-  __device__ __forceinline__ void flush(int nny) const {
-    for (int k = threadIdx.x; k < nrows * nnx; k += blockDim.x) {
-      const long long v = t64[k] + (long long)hi[k] * 65536 + (long long)lo[k];
-      const int r = row0 + k / nnx;
+  // fold + add the node sums to global memory; callers __syncthreads() before
+  __device__ __forceinline__ void flush(int nny) {
+    fold();
+    __syncthreads();
+    for (int k = threadIdx.x; k < (ncr + 1) * nnx; k += blockDim.x) {
+      const long long v = node[k];
+      const int r = crow0 + k / nnx;
       if (v != 0 && r >= 0 && r < nny)
         atomicAdd(&g[(size_t)r * nnx + (k % nnx)], (unsigned long long)v);
     }
   }
 };
 
-__host__ __device__ constexpr size_t rho_tile_bytes(int nrows, int nnx) {
-  return (size_t)nrows * nnx * (2 * sizeof(int) + sizeof(long long));
+__host__ __device__ constexpr size_t rho_moment_bytes(int ncr, int ncx) {
+  return (size_t)5 * ncr * ncx * sizeof(int) + (size_t)(ncr + 1) * (ncx + 1) * sizeof(long long);
 }
 
 // classification of a pushed particle listed in row s (s < 0: injected)
@@ -141,9 +172,8 @@ __global__ void k_init_particles(SimArgs a) {
 // ---------------------------------------------------------------------------
 __global__ void k_deposit(SimArgs a) {
   extern __shared__ long long dtile[];
-  const int s = blockIdx.x, nnx = a.nnx;
-  RhoTile T{reinterpret_cast<int *>(dtile + 2 * nnx), reinterpret_cast<int *>(dtile + 2 * nnx) + 2 * nnx,
-            dtile, s, 2, nnx, a.rho[a.ctl->cur]};
+  const int s = blockIdx.x, nnx = a.nnx, ncx = a.ncx;
+  RhoMoments T{reinterpret_cast<int *>(dtile + 2 * nnx), dtile, s, 1, ncx, nnx, a.rho[a.ctl->cur]};
   T.zero();
   __syncthreads();
   int since = 0;
@@ -225,7 +255,7 @@ constexpr int kCH = kPB * kPPT;
 }  // namespace
 
 size_t push_smem_bytes(int nnx) {
-  return (size_t)kStages * kCH * sizeof(float4) + rho_tile_bytes(4, nnx) +
+  return (size_t)kStages * kCH * sizeof(float4) + rho_moment_bytes(3, nnx - 1) +
          (size_t)2 * (nnx - 1) * sizeof(float4);
 }
 
@@ -237,10 +267,9 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
   const int nnx = a.nnx;
   const int ncx = a.ncx;
   float4 *stage = reinterpret_cast<float4 *>(push_raw);
-  float4 *etile = stage + kStages * kCH;                        // 2*ncx node pairs
-  long long *t64 = reinterpret_cast<long long *>(etile + 2 * ncx);  // 4 node rows s-1..s+2
-  int *thi = reinterpret_cast<int *>(t64 + 4 * nnx);
-  int *tlo = thi + 4 * nnx;
+  float4 *etile = stage + kStages * kCH;                          // 2*ncx node pairs
+  long long *tnode = reinterpret_cast<long long *>(etile + 2 * ncx);  // node rows s-1..s+2
+  int *tmom = reinterpret_cast<int *>(tnode + 4 * nnx);               // cell rows s-1..s+1
   __shared__ __align__(8) uint64_t full[kStages];
   __shared__ unsigned long long wsum[NE];
   __shared__ unsigned long long woff[NE];
@@ -269,7 +298,7 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
       bulk_g2s(stage + k * kCH, (sp1 ? row1 : row0) + (size_t)q * kCH, (uint32_t)cnt * 16u, &full[k]);
     }
   }
-  RhoTile T{thi, tlo, t64, s - 1, 4, nnx, a.rho[ctl->cur ^ 1]};
+  RhoMoments T{tmom, tnode, s - 1, 3, ncx, nnx, a.rho[ctl->cur ^ 1]};
   T.zero();
   for (int k = tid; k < 2 * ncx; k += kPB) {
     const int r = k / ncx, i = k - r * ncx;
@@ -391,7 +420,7 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
     }
     if ((k + 1) % (kFoldParticles / kCH) == 0 && k + 1 < nct) {  // block-uniform
       __syncthreads();
-      T.fold();
+      T.fold();  // the next deposits follow the next chunk's barriers
     }
   }
   for (int sp = 0; sp < 2; ++sp) {  // rows with no particles of a species
@@ -631,7 +660,7 @@ cudaError_t launch_init_particles(const SimArgs &a, cudaStream_t st) {
 }
 
 cudaError_t launch_deposit(const SimArgs &a, cudaStream_t st) {
-  k_deposit<<<a.ncy, 256, rho_tile_bytes(2, a.nnx), st>>>(a);
+  k_deposit<<<a.ncy, 256, rho_moment_bytes(1, a.ncx), st>>>(a);
   return cudaGetLastError();
 }
 
