@@ -62,6 +62,94 @@ __device__ __forceinline__ float block_max(float v, float *red) {
 
 }  // namespace
 
+struct SweepGeom {
+  int P, W, NG, TPR, RPI, gx, gy, lane;
+};
+
+// One Jacobi sweep of local rows [u0, u1) from S into D (mesh.cu:327-350):
+// v = 1/4 ((((b + west) + east) + north) + south), column nnx-1 mirroring
+// column 0 and the west neighbour of column 0 being column nnx-2.  Thread
+// (gx, gy) computes the 4 nodes 4gx..4gx+3 of rows u0+gy, u0+gy+RPI, ...;
+// its west/east neighbours come from the adjacent lanes by shuffle, or from
+// shared memory at the ends of a warp or a row.  The trip count is uniform
+// across each warp (rows advance by RPI from a common base), so the
+// shuffles always see all 32 lanes.  Returns the max |v - old| over owned
+// rows when CHECK.
+template <bool CHECK>
+__device__ __forceinline__ float sweep_vec(const float *__restrict__ S, float *__restrict__ D,
+                                           const float *__restrict__ bsrc, const SweepGeom &g, int u0,
+                                           int u1, int o0, int o1) {
+  const int P = g.P, W = g.W;
+  const int col = g.gx << 2;
+  const bool lfix = g.lane == 0 || g.gx == 0;
+  const bool rfix = g.lane == 31 || g.gx == g.TPR - 1;
+  const bool seam = g.gx == 0;
+  const int lcol = seam ? W - 1 : col - 1;
+  const bool active = g.gy < g.RPI;
+  float md = 0.0f;
+  for (int base = u0; base < u1; base += g.RPI) {
+    const int lr = base + g.gy;
+    const bool ok = active && lr < u1;
+    const float *rowp = S + lr * P;
+    float4 c4 = make_float4(0.f, 0.f, 0.f, 0.f), n4 = c4, s4 = c4, b4 = c4;
+    if (ok) {
+      c4 = *reinterpret_cast<const float4 *>(rowp + col);
+      n4 = *reinterpret_cast<const float4 *>(rowp + P + col);
+      s4 = *reinterpret_cast<const float4 *>(rowp - P + col);
+      b4 = *reinterpret_cast<const float4 *>(bsrc + lr * P + col);
+    }
+    float lf = __shfl_up_sync(0xffffffffu, c4.w, 1);
+    float rt = __shfl_down_sync(0xffffffffu, c4.x, 1);
+    if (ok) {
+      if (lfix) lf = rowp[lcol];
+      if (rfix) rt = rowp[col + 4];  // col+4 == W is the seam copy of node 0
+      float4 v;
+      v.x = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.x, lf), c4.y), n4.x), s4.x));
+      v.y = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.y, c4.x), c4.z), n4.y), s4.y));
+      v.z = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.z, c4.y), c4.w), n4.z), s4.z));
+      v.w = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.w, c4.z), rt), n4.w), s4.w));
+      float *dp = D + lr * P;
+      *reinterpret_cast<float4 *>(dp + col) = v;
+      if (seam) dp[W] = v.x;
+      if (CHECK && lr >= o0 && lr < o1) {
+        md = fmaxf(md, fabsf(__fsub_rn(v.x, c4.x)));
+        md = fmaxf(md, fabsf(__fsub_rn(v.y, c4.y)));
+        md = fmaxf(md, fabsf(__fsub_rn(v.z, c4.z)));
+        md = fmaxf(md, fabsf(__fsub_rn(v.w, c4.w)));
+        if (seam) md = fmaxf(md, fabsf(__fsub_rn(v.x, rowp[W])));
+      }
+    }
+  }
+  return md;
+}
+
+// the same sweep, one node per thread (used when (nnx-1) % 4 != 0)
+template <bool CHECK>
+__device__ __forceinline__ float sweep_scalar(const float *__restrict__ S, float *__restrict__ D,
+                                              const float *__restrict__ bsrc, const SweepGeom &g,
+                                              int u0, int u1, int o0, int o1) {
+  const int P = g.P, W = g.W;
+  float md = 0.0f;
+  if (g.gy >= g.RPI) return md;
+  for (int lr = u0 + g.gy; lr < u1; lr += g.RPI) {
+    const float *cr = S + lr * P;
+    for (int i = g.gx; i < W; i += g.TPR) {
+      const float wv = (i == 0) ? cr[W - 1] : cr[i - 1];
+      const float v = __fmul_rn(
+          0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(bsrc[lr * P + i], wv), cr[i + 1]), cr[P + i]),
+                           cr[i - P]));
+      D[lr * P + i] = v;
+      const bool own = CHECK && lr >= o0 && lr < o1;
+      if (own) md = fmaxf(md, fabsf(__fsub_rn(v, cr[i])));
+      if (i == 0) {
+        D[lr * P + W] = v;
+        if (own) md = fmaxf(md, fabsf(__fsub_rn(v, cr[W])));
+      }
+    }
+  }
+  return md;
+}
+
 // Rows of CTA c: interior rows [r0, r1) with r0 = 1 + c*M/G (M = nny-2), so
 // every CTA owns floor(M/G) or ceil(M/G) rows.  With temporal blocking depth
 // k, a CTA also holds k halo rows on each side; sweep m (1..k) after an
@@ -105,80 +193,33 @@ __global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) 
   __syncthreads();
 
   const int W = nnx - 1;  // computed columns 0 .. nnx-2; column nnx-1 mirrors 0
-  // thread -> (column group gx, row offset gy), fixed for the whole solve.
-  // Vector path: a group is 4 consecutive nodes (float4); scalar path: 1.
   const bool vec = J.vec != 0;
-  const int NG = vec ? (W >> 2) : W;           // column groups per row
-  const int TPR = min(NG, kJBlock);            // threads per row
-  const int RPI = kJBlock / TPR;               // rows per iteration
-  const int gx = tid % TPR, gy = tid / TPR;
-  const int lane = tid & 31;
-  const int iters_c = (NG + TPR - 1) / TPR;
-  int src = 0, done = 0, nchk = 0;
+  SweepGeom sg;
+  sg.P = P;
+  sg.W = W;
+  sg.NG = vec ? (W >> 2) : W;  // column groups per row (4 nodes each on the vector path)
+  sg.TPR = min(sg.NG, kJBlock);
+  sg.RPI = kJBlock / sg.TPR;
+  sg.gx = tid % sg.TPR;
+  sg.gy = tid / sg.TPR;
+  sg.lane = tid & 31;
+  int src = 0, done = 0, nchk = 0, m = 0;
   float last = INFINITY;
   for (int s = 1; s <= J.max_sweeps; ++s) {
     const float *S = buf[src];
     float *D = buf[src ^ 1];
     const bool check = (s % J.check_every == 0) || (s == J.max_sweeps);
-    const int m = G > 1 ? ((s - 1) % K) + 1 : 1;
+    m = (m >= K) ? 1 : m + 1;                        // position in the temporal block
     const int u0 = max(1, r0 - K + m) - lo;          // updated local rows [u0, u1)
     const int u1 = min(nny - 2, r1 - 1 + K - m) + 1 - lo;
     const int o0 = r0 - lo, o1 = r1 - lo;            // owned local rows
     float md = 0.0f;
-    const int iters_r = (u1 - u0 + RPI - 1) / RPI;
-    for (int ir = 0; ir < iters_r; ++ir) {
-      const int lr = u0 + gy + ir * RPI;
-      const bool rowok = gy < RPI && lr < u1;
-      const bool own = check && rowok && lr >= o0 && lr < o1;
-      const float *cr = S + lr * P;
-      for (int ic = 0; ic < iters_c; ++ic) {
-        const int cg = gx + ic * TPR;
-        const bool ok = rowok && cg < NG;
-        if (vec) {
-          const int col = cg << 2;
-          float4 c4 = make_float4(0.f, 0.f, 0.f, 0.f), n4 = c4, s4 = c4, b4 = c4;
-          if (ok) {
-            c4 = *reinterpret_cast<const float4 *>(cr + col);
-            n4 = *reinterpret_cast<const float4 *>(cr + P + col);
-            s4 = *reinterpret_cast<const float4 *>(cr - P + col);
-            b4 = *reinterpret_cast<const float4 *>(bsrc + lr * P + col);
-          }
-          float lf = __shfl_up_sync(0xffffffffu, c4.w, 1);
-          float rt = __shfl_down_sync(0xffffffffu, c4.x, 1);
-          if (ok) {
-            // neighbours not held by the adjacent lane come from shared memory;
-            // west of node 0 is node nnx-2, east of node nnx-2 is the seam copy
-            if (lane == 0 || gx == 0) lf = cg == 0 ? cr[W - 1] : cr[col - 1];
-            if (lane == 31 || gx == TPR - 1 || cg == NG - 1) rt = cr[col + 4];
-            float4 v;
-            v.x = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.x, lf), c4.y), n4.x), s4.x));
-            v.y = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.y, c4.x), c4.z), n4.y), s4.y));
-            v.z = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.z, c4.y), c4.w), n4.z), s4.z));
-            v.w = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.w, c4.z), rt), n4.w), s4.w));
-            *reinterpret_cast<float4 *>(D + lr * P + col) = v;
-            if (cg == 0) D[lr * P + W] = v.x;
-            if (own) {
-              md = fmaxf(md, fabsf(__fsub_rn(v.x, c4.x)));
-              md = fmaxf(md, fabsf(__fsub_rn(v.y, c4.y)));
-              md = fmaxf(md, fabsf(__fsub_rn(v.z, c4.z)));
-              md = fmaxf(md, fabsf(__fsub_rn(v.w, c4.w)));
-              if (cg == 0) md = fmaxf(md, fabsf(__fsub_rn(v.x, cr[W])));
-            }
-          }
-        } else if (ok) {
-          const int i = cg;
-          const float wv = (i == 0) ? cr[W - 1] : cr[i - 1];
-          const float v = __fmul_rn(
-              0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(bsrc[lr * P + i], wv), cr[i + 1]), cr[P + i]),
-                               cr[i - P]));
-          D[lr * P + i] = v;
-          if (own) md = fmaxf(md, fabsf(__fsub_rn(v, cr[i])));
-          if (i == 0) {
-            D[lr * P + W] = v;
-            if (own) md = fmaxf(md, fabsf(__fsub_rn(v, cr[W])));
-          }
-        }
-      }
+    if (vec) {
+      if (check) md = sweep_vec<true>(S, D, bsrc, sg, u0, u1, o0, o1);
+      else sweep_vec<false>(S, D, bsrc, sg, u0, u1, o0, o1);
+    } else {
+      if (check) md = sweep_scalar<true>(S, D, bsrc, sg, u0, u1, o0, o1);
+      else sweep_scalar<false>(S, D, bsrc, sg, u0, u1, o0, o1);
     }
     __syncthreads();
     if (G > 1 && m == K) {
