@@ -196,7 +196,7 @@ int plan_jacobi(cupic_ctx *c) {
   }
   G = std::max(1, std::min(G, M));
   int B = (M + G - 1) / G;
-  if (K <= 0) K = 4;
+  if (K <= 0) K = 8;
   K = std::max(1, std::min(K, M / G));
   if (G == 1) K = 1;
   while (G > 1 && B + 2 * K > rows_fit) {  // shrink the depth, then add CTAs

@@ -38,7 +38,7 @@ __device__ bool wait_geq(const unsigned *p, unsigned v, Ctl *ctl) {
   for (long long it = 0; it < kSpinLimit; ++it) {
     if (ld_acquire(p) >= v) return true;
     if ((it & 255) == 255 && *(volatile int *)&ctl->abort) return false;
-    if (it > 32) __nanosleep(64);
+    if (it > 4096) __nanosleep(32);
   }
   atomicExch(&ctl->abort, 1);
   atomicOr(&ctl->step_flags, (uint32_t)CUPIC_FLAG_TIMEOUT);
@@ -170,25 +170,26 @@ __global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) 
   const int hi = min(nny - 1, r1 - 1 + K);   // last buffered row
   const int nrows = hi - lo + 1;
   const int cap = J.rows_per_cta + 2 * K;    // buffer rows reserved per array
-  float *buf[2] = {jsm, jsm + (size_t)cap * P};
-  float *bsrc = jsm + (size_t)2 * cap * P;   // same row indexing as buf
+  float *const buf0 = jsm;
+  float *const buf1 = jsm + (size_t)cap * P;
+  float *const bsrc = jsm + (size_t)2 * cap * P;  // same row indexing as the buffers
   Ctl *ctl = a.ctl;
   if (tid == 0) bail = 0;
 
-  for (int k = tid; k < nrows * nnx; k += kJBlock) {
-    const int lr = k / nnx, i = k - lr * nnx;
-    const float v = a.phi[(size_t)(lo + lr) * nnx + i];
-    buf[0][lr * P + i] = v;
-    buf[1][lr * P + i] = v;
-  }
   const long long *acc = reinterpret_cast<const long long *>(a.rho[ctl->cur]);
-  for (int k = tid; k < nrows * nnx; k += kJBlock) {
-    const int lr = k / nnx, i = k - lr * nnx;
+  for (int lr = 0; lr < nrows; ++lr) {
     const int j = lo + lr;
-    if (j < 1 || j > nny - 2) continue;
     const size_t rb = (size_t)j * nnx;
-    const long long f = (i == 0 || i == nnx - 1) ? acc[rb] + acc[rb + nnx - 1] : acc[rb + i];
-    bsrc[lr * P + i] = __double2float_rn((double)f * a.cb);
+    const bool interior = j >= 1 && j <= nny - 2;
+    for (int i = tid; i < nnx; i += kJBlock) {
+      const float v = a.phi[rb + i];
+      buf0[lr * P + i] = v;
+      buf1[lr * P + i] = v;
+      if (interior) {
+        const long long f = (i == 0 || i == nnx - 1) ? acc[rb] + acc[rb + nnx - 1] : acc[rb + i];
+        bsrc[lr * P + i] = __double2float_rn((double)f * a.cb);
+      }
+    }
   }
   __syncthreads();
 
@@ -203,59 +204,75 @@ __global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) 
   sg.gx = tid % sg.TPR;
   sg.gy = tid / sg.TPR;
   sg.lane = tid & 31;
-  int src = 0, done = 0, nchk = 0, m = 0;
-  float last = INFINITY;
-  for (int s = 1; s <= J.max_sweeps; ++s) {
-    const float *S = buf[src];
-    float *D = buf[src ^ 1];
-    const bool check = (s % J.check_every == 0) || (s == J.max_sweeps);
-    m = (m >= K) ? 1 : m + 1;                        // position in the temporal block
-    const int u0 = max(1, r0 - K + m) - lo;          // updated local rows [u0, u1)
-    const int u1 = min(nny - 2, r1 - 1 + K - m) + 1 - lo;
-    const int o0 = r0 - lo, o1 = r1 - lo;            // owned local rows
-    float md = 0.0f;
-    if (vec) {
-      if (check) md = sweep_vec<true>(S, D, bsrc, sg, u0, u1, o0, o1);
-      else sweep_vec<false>(S, D, bsrc, sg, u0, u1, o0, o1);
-    } else {
-      if (check) md = sweep_scalar<true>(S, D, bsrc, sg, u0, u1, o0, o1);
-      else sweep_scalar<false>(S, D, bsrc, sg, u0, u1, o0, o1);
-    }
-    __syncthreads();
-    if (G > 1 && m == K) {
-      const int e = s / K;  // exchange number
-      float *hp = J.halo + ((size_t)(e & 1) * G + c) * 2 * K * P;
-      for (int k = tid; k < K * nnx; k += kJBlock) {
-        const int r = k / nnx, i = k - r * nnx;
+  const int o0 = r0 - lo, o1 = r1 - lo;  // owned local rows
+  auto sweep = [&](const float *S, float *D, int u0, int u1, bool check) -> float {
+    if (u0 >= u1) return 0.0f;
+    if (vec) return check ? sweep_vec<true>(S, D, bsrc, sg, u0, u1, o0, o1)
+                          : sweep_vec<false>(S, D, bsrc, sg, u0, u1, o0, o1);
+    return check ? sweep_scalar<true>(S, D, bsrc, sg, u0, u1, o0, o1)
+                 : sweep_scalar<false>(S, D, bsrc, sg, u0, u1, o0, o1);
+  };
+  // halo exchange, split in two so the rows that need no halo can be swept
+  // while the neighbours' rows are in flight
+  auto publish = [&](const float *D, int e) {
+    float *hp = J.halo + ((size_t)(e & 1) * G + c) * 2 * K * P;
+    for (int r = 0; r < K; ++r)
+      for (int i = tid; i < nnx; i += kJBlock) {
         __stcg(hp + r * P + i, D[(o0 + r) * P + i]);
         __stcg(hp + (K + r) * P + i, D[(o1 - K + r) * P + i]);
       }
-      __syncthreads();
-      if (tid == 0) {
-        __threadfence();
-        st_release(&J.flags[c], (unsigned)e);
-        bool ok = true;
-        if (c > 0) ok = wait_geq(&J.flags[c - 1], (unsigned)e, ctl);
-        if (ok && c < G - 1) ok = wait_geq(&J.flags[c + 1], (unsigned)e, ctl);
-        if (!ok) bail = 1;
-      }
-      __syncthreads();
-      if (bail) break;
-      if (c > 0) {  // rows [r0-K, r0) = the lower neighbour's last K rows
-        const float *hn = J.halo + ((size_t)(e & 1) * G + (c - 1)) * 2 * K * P + K * P;
-        for (int k = tid; k < K * nnx; k += kJBlock) {
-          const int r = k / nnx, i = k - r * nnx;
-          D[(o0 - K + r) * P + i] = __ldcg(hn + r * P + i);
-        }
-      }
-      if (c < G - 1) {  // rows [r1, r1+K) = the upper neighbour's first K rows
-        const float *hn = J.halo + ((size_t)(e & 1) * G + (c + 1)) * 2 * K * P;
-        for (int k = tid; k < K * nnx; k += kJBlock) {
-          const int r = k / nnx, i = k - r * nnx;
-          D[(o1 + r) * P + i] = __ldcg(hn + r * P + i);
-        }
-      }
-      __syncthreads();
+    __syncthreads();
+    if (tid == 0) st_release(&J.flags[c], (unsigned)e);
+  };
+  auto receive = [&](float *D, int e) -> bool {
+    if (tid == 0) {
+      bool ok = true;
+      if (c > 0) ok = wait_geq(&J.flags[c - 1], (unsigned)e, ctl);
+      if (ok && c < G - 1) ok = wait_geq(&J.flags[c + 1], (unsigned)e, ctl);
+      if (!ok) bail = 1;
+    }
+    __syncthreads();
+    if (bail) return false;
+    if (c > 0) {  // rows [r0-K, r0) = the lower neighbour's last K rows
+      const float *hn = J.halo + ((size_t)(e & 1) * G + (c - 1)) * 2 * K * P + K * P;
+      for (int r = 0; r < K; ++r)
+        for (int i = tid; i < nnx; i += kJBlock) D[(o0 - K + r) * P + i] = __ldcg(hn + r * P + i);
+    }
+    if (c < G - 1) {  // rows [r1, r1+K) = the upper neighbour's first K rows
+      const float *hn = J.halo + ((size_t)(e & 1) * G + (c + 1)) * 2 * K * P;
+      for (int r = 0; r < K; ++r)
+        for (int i = tid; i < nnx; i += kJBlock) D[(o1 + r) * P + i] = __ldcg(hn + r * P + i);
+    }
+    __syncthreads();
+    return true;
+  };
+
+  int src = 0, done = 0, nchk = 0, m = 0, pending = 0, to_check = J.check_every;
+  float last = INFINITY;
+  for (int s = 1; s <= J.max_sweeps; ++s) {
+    float *S = src ? buf1 : buf0;
+    float *D = src ? buf0 : buf1;
+    const bool check = (--to_check == 0) || (s == J.max_sweeps);
+    if (to_check == 0) to_check = J.check_every;
+    m = (m >= K) ? 1 : m + 1;                        // position in the temporal block
+    const int u0 = max(1, r0 - K + m) - lo;          // updated local rows [u0, u1)
+    const int u1 = min(nny - 2, r1 - 1 + K - m) + 1 - lo;
+    float md;
+    if (pending) {
+      // rows o0+1 .. o1-2 read only owned rows of S: sweep them first
+      const int i0 = max(u0, o0 + 1), i1 = min(u1, o1 - 1);
+      md = sweep(S, D, i0, i1, check);
+      if (!receive(S, pending)) break;
+      md = fmaxf(md, sweep(S, D, u0, min(i0, u1), check));
+      md = fmaxf(md, sweep(S, D, max(i1, u0), u1, check));
+      pending = 0;
+    } else {
+      md = sweep(S, D, u0, u1, check);
+    }
+    __syncthreads();
+    if (G > 1 && m == K) {
+      publish(D, s / K);
+      pending = s / K;
     }
     src ^= 1;
     done = s;
@@ -279,27 +296,26 @@ __global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) 
       if (s >= J.min_sweeps && (double)bm < J.tol) break;
     }
   }
+  float *F = src ? buf1 : buf0;
+  if (pending && !bail) receive(F, pending);
 
   // write back the owned rows; derive E = -grad phi (mesh.cu:413-468).  The
   // rows r0-1 and r1 are current: either just exchanged or updated in the
   // last sweep of an unfinished temporal block.
-  const float *F = buf[src];
-  const int o0 = r0 - lo, o1 = r1 - lo;
-  for (int k = tid; k < (o1 - o0) * nnx; k += kJBlock) {
-    const int lr = k / nnx + o0, i = k - (lr - o0) * nnx;
-    a.phi[(size_t)(lo + lr) * nnx + i] = F[lr * P + i];
-  }
+  for (int lr = o0; lr < o1; ++lr)
+    for (int i = tid; i < nnx; i += kJBlock) a.phi[(size_t)(lo + lr) * nnx + i] = F[lr * P + i];
   if (J.do_field) {
-    for (int k = tid; k < (o1 - o0) * nnx; k += kJBlock) {
-      const int lr = k / nnx + o0, i = k - (lr - o0) * nnx;
+    for (int lr = o0; lr < o1; ++lr) {
       const float *cr = F + lr * P;
-      const bool seam = (i == 0 || i == nnx - 1);
-      const float wv = seam ? cr[nnx - 2] : cr[i - 1];
-      const float ev = seam ? cr[1] : cr[i + 1];
-      float2 e;
-      e.x = __fdiv_rn(__fsub_rn(wv, ev), a.two_ds);
-      e.y = __fdiv_rn(__fsub_rn(cr[i - P], cr[i + P]), a.two_ds);
-      a.E[(size_t)(lo + lr) * nnx + i] = e;
+      for (int i = tid; i < nnx; i += kJBlock) {
+        const bool seam = (i == 0 || i == nnx - 1);
+        const float wv = seam ? cr[nnx - 2] : cr[i - 1];
+        const float ev = seam ? cr[1] : cr[i + 1];
+        float2 e;
+        e.x = __fdiv_rn(__fsub_rn(wv, ev), a.two_ds);
+        e.y = __fdiv_rn(__fsub_rn(cr[i - P], cr[i + P]), a.two_ds);
+        a.E[(size_t)(lo + lr) * nnx + i] = e;
+      }
     }
     if (c == 0) {
       for (int i = tid; i < nnx; i += kJBlock)
