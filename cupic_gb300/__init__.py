@@ -33,7 +33,7 @@ EXPORTED = [
     "cupic_get_counts", "cupic_store_particles", "cupic_store_particles_f32",
     "cupic_get_bookmarks", "cupic_get_rho", "cupic_get_rho_fixed", "cupic_get_phi",
     "cupic_set_phi", "cupic_get_field", "cupic_get_phi_f32", "cupic_get_field_f32",
-    "cupic_get_stats", "cupic_get_flags", "cupic_clear_flags",
+    "cupic_get_stats", "cupic_get_flags", "cupic_clear_flags", "cupic_poisson_solver_static",
 ]
 
 
@@ -94,6 +94,9 @@ def load_library(build_if_missing=False):
         "cupic_get_stats": [vp, P(StepStats), c_i32],
         "cupic_get_flags": [vp, P(ctypes.c_uint32)],
         "cupic_clear_flags": [vp],
+        "cupic_poisson_solver_static": [P(Params), ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_void_p, c_d, c_i32, c_i32, c_i32,
+                                        ctypes.c_void_p, P(c_i32), P(ctypes.c_float)],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

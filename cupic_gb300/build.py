@@ -16,7 +16,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcupic_gpu.so")
-SOURCES = ["capi.cu", "particles.cu", "jacobi.cu", "io.cu"]
+SOURCES = ["capi.cu", "particles.cu", "jacobi.cu", "io.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

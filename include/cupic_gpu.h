@@ -210,6 +210,33 @@ int cupic_get_stats(struct cupic_ctx *ctx, cupic_step_stats *out, int32_t count)
 int cupic_get_flags(struct cupic_ctx *ctx, uint32_t *flags);
 int cupic_clear_flags(struct cupic_ctx *ctx);
 
+/* ---- solve without allocating ------------------------------------------ */
+
+/* The Poisson solve (and field) on caller-owned DEVICE buffers, allocating
+ * nothing.  It has no counterpart in the reference.  It is for callers that
+ * cannot call cudaMalloc: code inside a stream capture, real-time loops that
+ * forbid allocation, hosts whose device memory comes from their own pool.
+ *   rho_dev  nnx*nny raw int64 fixed-point charge (2^32 per unit charge, the
+ *            layout of cupic_get_rho_fixed, columns 0 and nnx-1 not folded)
+ *   phi_dev  nnx*nny float potential, read as the initial guess, overwritten
+ *   e_dev    nnx*nny {Ex, Ey} float pairs, written; NULL skips the field
+ *   stream   a cudaStream_t, NULL for the default stream; the call waits for
+ *            its own work before returning
+ * The solver's scratch (sweep counters, residual slots and the halo rows its
+ * CTAs trade) lives in a static 4 MiB device array that every GPU loading
+ * this library holds until exit.  The call lowers the halo depth, then the
+ * CTA count, until the scratch fits; meshes for which nothing fits return
+ * CUPIC_ERR_CAPACITY.  The largest ncy accepted is 5321 at ncx = 512, 2433
+ * at ncx = 1024, 890 at ncx = 2048 and 127 at ncx = 4096.  The first call on a device
+ * looks the array up (cudaGetSymbolAddress); make that first call before any
+ * stream capture.  All calls share the array and it keeps the last call's
+ * contents: calls that overlap on the GPU (other streams, other host
+ * threads) race and must be serialised by the caller. */
+int cupic_poisson_solver_static(const cupic_params *p, const int64_t *rho_dev, float *phi_dev,
+                                float *e_dev, double max_error, int32_t min_sweeps,
+                                int32_t max_sweeps, int32_t check_every, void *stream,
+                                int32_t *sweeps_out, float *residual_out);
+
 #ifdef __cplusplus
 }
 #endif
