@@ -1,0 +1,68 @@
+"""Build and run the reference's own input_data getters (src/init.cu:424-789).
+
+TEST INFRASTRUCTURE ONLY.  The reference's sources are compiled where they
+lie (REF_SRC below) with nvcc into oracle/_ref/ -- never copied -- together with:
+- a project-written GSL API shim (ref_pin/gsl*, written from the math);
+- a forced include that renames mesh.cu's own double atomicAdd, which sm_60+
+  already defines (defect D1);
+- a harness (ref_pin/pin_main.cpp) that calls the getters and prints every
+  derived parameter as exact hex doubles.
+No GPU is needed: only host functions run.
+"""
+import json
+import os
+import shutil
+import subprocess
+import tempfile
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PIN = os.path.join(HERE, "ref_pin")
+OUT = os.path.join(HERE, "_ref")
+BIN = os.path.join(OUT, "ref_pin")
+REF_SRC = "/root/reference/src"
+UNITS = ["init", "cc", "particles", "diagnostic", "cuda", "mesh"]
+
+
+def available():
+    return os.path.isdir(REF_SRC) and shutil.which("nvcc") is not None
+
+
+def build(force=False):
+    """Compile oracle/_ref/ref_pin when the reference sources are present."""
+    if not available():
+        return None
+    if os.path.exists(BIN) and not force:
+        return BIN
+    obj = os.path.join(OUT, "obj")
+    os.makedirs(obj, exist_ok=True)
+    flags = ["-gencode", "arch=compute_103a,code=sm_103a", "-dc", "-I", PIN, "-w"]
+    procs = []
+    for u in UNITS:
+        extra = ["-include", os.path.join(PIN, "d1_guard.h")] if u == "mesh" else []
+        procs.append(subprocess.Popen(["nvcc"] + flags + extra +
+                                      [os.path.join(REF_SRC, u + ".cu"), "-o", os.path.join(obj, u + ".o")]))
+    for p in procs:
+        if p.wait() != 0:
+            raise RuntimeError("nvcc failed on a reference source")
+    subprocess.run(["g++", "-O0", "-c", os.path.join(PIN, "gsl_shim.cpp"), "-I", PIN, "-o",
+                    os.path.join(obj, "gsl_shim.o")], check=True)
+    subprocess.run(["g++", "-O0", "-c", os.path.join(PIN, "pin_main.cpp"), "-o",
+                    os.path.join(obj, "pin_main.o")], check=True)
+    objs = [os.path.join(obj, u + ".o") for u in UNITS + ["gsl_shim", "pin_main"]]
+    subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a"] + objs + ["-o", BIN],
+                   check=True)
+    return BIN
+
+
+def run(input_text):
+    """Derived parameters of one input_data text, from the reference's code."""
+    exe = build()
+    if exe is None:
+        raise RuntimeError("reference sources not available")
+    with tempfile.TemporaryDirectory() as d:
+        os.makedirs(os.path.join(d, "input"))
+        os.makedirs(os.path.join(d, "run"))
+        with open(os.path.join(d, "input", "input_data"), "w") as f:
+            f.write(input_text)
+        out = subprocess.run([exe, d], capture_output=True, text=True, check=True).stdout
+    return json.loads(out)
