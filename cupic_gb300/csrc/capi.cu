@@ -234,7 +234,9 @@ JacobiArgs jargs(const cupic_ctx *c, double tol, int mn, int mx, int chk, int fi
   J.depth = c->jK;
   J.pitch = c->jP;
   J.vec = ((c->a.nnx - 1) % 4 == 0) ? 1 : 0;
+  J.strip = jacobi_strip_rows(c->a.nnx, c->jB + 2 * (c->jG > 1 ? c->jK : 1) - 2);
   if (getenv("CUPIC_JACOBI_SCALAR")) J.vec = 0;
+  if (getenv("CUPIC_JACOBI_SCALAR") || getenv("CUPIC_JACOBI_NOSTRIP")) J.strip = 0;
   J.do_field = field;
   J.write_stats = 1;
   J.flags = c->jflags;

@@ -86,6 +86,7 @@ struct JacobiArgs {
   int32_t depth;          // temporal blocking: sweeps between halo exchanges (G > 1)
   int32_t pitch;          // smem row pitch in floats (a multiple of 4)
   int32_t vec;            // 1: (nnx-1) % 4 == 0, sweep 4 nodes per thread with float4
+  int32_t strip;          // 0: shared-memory sweep; 1, 2, 4, 8: rows kept in registers per thread
   int32_t do_field;       // 1: derive E after the last sweep
   int32_t write_stats;    // 1: store sweeps/residual in the control block
   unsigned int *flags;    // [G] last sweep published by each CTA

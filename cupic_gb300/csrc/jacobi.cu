@@ -20,7 +20,8 @@ namespace cupic {
 
 namespace {
 
-constexpr int kJBlock = 1024;
+constexpr int kJBlock = 512;
+constexpr int kMaxDepth = 8;  // largest temporal-blocking depth
 constexpr long long kSpinLimit = 1ll << 22;
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
@@ -150,16 +151,83 @@ __device__ __forceinline__ float sweep_scalar(const float *__restrict__ S, float
   return md;
 }
 
+// Register-strip sweep (used when (nnx-1) % 4 == 0 and the CTA's rows fit):
+// thread (gx, gy) keeps the 4 nodes 4gx..4gx+3 of the R consecutive rows
+// lr0 .. lr0+R-1 (lr0 = 1 + gy*R) in registers for the whole solve, with their
+// source terms.  A sweep then reads from shared memory only the rows just
+// below and above the strip and the west/east values at the ends of a warp
+// or a row; the strip's own rows come from registers and its west/east
+// neighbours by shuffle.  Every updated row is still stored to D, where the
+// neighbouring strips, lanes and the halo exchange find it.  Rows outside
+// [u0, u1) keep their registers unchanged, exactly as the shared-memory
+// path leaves them unwritten.
+struct RegGeom {
+  int P, W, NG, gx, gy, lane, lr0, nvalid, col, lcol;
+  bool active, lfix, rfix, seam;
+};
+
+__device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+
+template <int R, bool CHECK>
+__device__ __forceinline__ float sweep_reg(float4 (&x)[R], const float4 (&b)[R], const float *__restrict__ S,
+                                           float *__restrict__ D, const RegGeom &g, int u0, int u1, int o0,
+                                           int o1) {
+  const int P = g.P, W = g.W, col = g.col;
+  float4 s4 = make_float4(0.f, 0.f, 0.f, 0.f), n4 = s4;
+  if (g.active && g.nvalid > 0) {
+    s4 = lds4(S + (g.lr0 - 1) * P + col);
+    n4 = lds4(S + (g.lr0 + g.nvalid) * P + col);
+  }
+  float4 prev = s4;
+  float md = 0.0f;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const float4 c = x[r];
+    float lf = __shfl_up_sync(0xffffffffu, c.w, 1);
+    float rt = __shfl_down_sync(0xffffffffu, c.x, 1);
+    const int lr = g.lr0 + r;
+    if (g.active && r < g.nvalid) {
+      const float *rowp = S + lr * P;
+      if (g.lfix) lf = rowp[g.lcol];
+      if (g.rfix) rt = rowp[col + 4];
+      if (lr >= u0 && lr < u1) {
+        float4 nb = n4;
+        if (r + 1 < R && r + 1 < g.nvalid) nb = x[r + 1 < R ? r + 1 : r];
+        float4 v;
+        v.x = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].x, lf), c.y), nb.x), prev.x));
+        v.y = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].y, c.x), c.z), nb.y), prev.y));
+        v.z = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].z, c.y), c.w), nb.z), prev.z));
+        v.w = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].w, c.z), rt), nb.w), prev.w));
+        float *dp = D + lr * P;
+        *reinterpret_cast<float4 *>(dp + col) = v;
+        if (g.seam) dp[W] = v.x;
+        if (CHECK && lr >= o0 && lr < o1) {
+          md = fmaxf(md, fabsf(__fsub_rn(v.x, c.x)));
+          md = fmaxf(md, fabsf(__fsub_rn(v.y, c.y)));
+          md = fmaxf(md, fabsf(__fsub_rn(v.z, c.z)));
+          md = fmaxf(md, fabsf(__fsub_rn(v.w, c.w)));
+          if (g.seam) md = fmaxf(md, fabsf(__fsub_rn(v.x, rowp[W])));
+        }
+        x[r] = v;
+      }
+    }
+    prev = c;  // the previous value of row r is the south neighbour of row r+1
+  }
+  return md;
+}
+
 // Rows of CTA c: interior rows [r0, r1) with r0 = 1 + c*M/G (M = nny-2), so
 // every CTA owns floor(M/G) or ceil(M/G) rows.  With temporal blocking depth
 // k, a CTA also holds k halo rows on each side; sweep m (1..k) after an
 // exchange updates the rows [r0-k+m, r1+k-m) -- the halo part redundantly,
 // with the same operands as the neighbour, so the values are identical --
 // and the neighbours trade their k boundary rows only every k sweeps.
-__global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) {
-  extern __shared__ float jsm[];
-  __shared__ float red[33];
-  __shared__ int bail;
+// R > 0 selects the register-strip sweep with strips of R rows; R == 0 the
+// shared-memory sweep (sweep_vec / sweep_scalar).
+template <int R>
+__device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &J, float *jsm, float *red,
+                                            int *bail_p) {
+  int &bail = *bail_p;
   const int c = blockIdx.x, G = J.G, tid = threadIdx.x;
   const int nnx = a.nnx, nny = a.nny, P = J.pitch;
   const int M = nny - 2;
@@ -174,7 +242,6 @@ __global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) 
   float *const buf1 = jsm + (size_t)cap * P;
   float *const bsrc = jsm + (size_t)2 * cap * P;  // same row indexing as the buffers
   Ctl *ctl = a.ctl;
-  if (tid == 0) bail = 0;
 
   const long long *acc = reinterpret_cast<const long long *>(a.rho[ctl->cur]);
   for (int lr = 0; lr < nrows; ++lr) {
@@ -194,33 +261,72 @@ __global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) 
   __syncthreads();
 
   const int W = nnx - 1;  // computed columns 0 .. nnx-2; column nnx-1 mirrors 0
+  const int o0 = r0 - lo, o1 = r1 - lo;  // owned local rows
+  // shared-memory sweep geometry (R == 0)
   const bool vec = J.vec != 0;
   SweepGeom sg;
   sg.P = P;
   sg.W = W;
-  sg.NG = vec ? (W >> 2) : W;  // column groups per row (4 nodes each on the vector path)
+  sg.NG = vec ? (W >> 2) : W;
   sg.TPR = min(sg.NG, kJBlock);
   sg.RPI = kJBlock / sg.TPR;
   sg.gx = tid % sg.TPR;
   sg.gy = tid / sg.TPR;
   sg.lane = tid & 31;
-  const int o0 = r0 - lo, o1 = r1 - lo;  // owned local rows
+  // register-strip geometry (R > 0)
+  RegGeom rg;
+  float4 x[R > 0 ? R : 1], bb[R > 0 ? R : 1];
+  if (R > 0) {
+    rg.P = P;
+    rg.W = W;
+    rg.NG = W >> 2;
+    rg.gx = tid % rg.NG;
+    rg.gy = tid / rg.NG;
+    rg.lane = tid & 31;
+    rg.lr0 = 1 + rg.gy * R;
+    rg.active = rg.lr0 < nrows - 1;
+    rg.nvalid = rg.active ? min(R, nrows - 1 - rg.lr0) : 0;
+    rg.col = rg.gx << 2;
+    rg.seam = rg.gx == 0;
+    rg.lcol = rg.seam ? W - 1 : rg.col - 1;
+    rg.lfix = rg.lane == 0 || rg.gx == 0;
+    rg.rfix = rg.lane == 31 || rg.gx == rg.NG - 1;
+#pragma unroll
+    for (int r = 0; r < (R > 0 ? R : 1); ++r) {
+      x[r] = make_float4(0.f, 0.f, 0.f, 0.f);
+      bb[r] = x[r];
+      if (r < rg.nvalid) {
+        x[r] = lds4(buf0 + (rg.lr0 + r) * P + rg.col);
+        bb[r] = lds4(bsrc + (rg.lr0 + r) * P + rg.col);
+      }
+    }
+  }
   auto sweep = [&](const float *S, float *D, int u0, int u1, bool check) -> float {
-    if (u0 >= u1) return 0.0f;
-    if (vec) return check ? sweep_vec<true>(S, D, bsrc, sg, u0, u1, o0, o1)
-                          : sweep_vec<false>(S, D, bsrc, sg, u0, u1, o0, o1);
-    return check ? sweep_scalar<true>(S, D, bsrc, sg, u0, u1, o0, o1)
-                 : sweep_scalar<false>(S, D, bsrc, sg, u0, u1, o0, o1);
+    if constexpr (R > 0) {
+      return check ? sweep_reg<R, true>(x, bb, S, D, rg, u0, u1, o0, o1)
+                   : sweep_reg<R, false>(x, bb, S, D, rg, u0, u1, o0, o1);
+    } else {
+      if (u0 >= u1) return 0.0f;
+      if (vec) return check ? sweep_vec<true>(S, D, bsrc, sg, u0, u1, o0, o1)
+                            : sweep_vec<false>(S, D, bsrc, sg, u0, u1, o0, o1);
+      return check ? sweep_scalar<true>(S, D, bsrc, sg, u0, u1, o0, o1)
+                   : sweep_scalar<false>(S, D, bsrc, sg, u0, u1, o0, o1);
+    }
   };
-  // halo exchange, split in two so the rows that need no halo can be swept
-  // while the neighbours' rows are in flight
+  // Halo exchange.  The K rows of each side move as one batch per column
+  // block (all loads issued before the first store), so a transfer costs one
+  // L2 round trip rather than K.
   auto publish = [&](const float *D, int e) {
     float *hp = J.halo + ((size_t)(e & 1) * G + c) * 2 * K * P;
-    for (int r = 0; r < K; ++r)
-      for (int i = tid; i < nnx; i += kJBlock) {
-        __stcg(hp + r * P + i, D[(o0 + r) * P + i]);
-        __stcg(hp + (K + r) * P + i, D[(o1 - K + r) * P + i]);
+    for (int i = tid; i < nnx; i += kJBlock) {
+#pragma unroll
+      for (int r = 0; r < kMaxDepth; ++r) {
+        if (r < K) {
+          __stcg(hp + r * P + i, D[(o0 + r) * P + i]);
+          __stcg(hp + (K + r) * P + i, D[(o1 - K + r) * P + i]);
+        }
       }
+    }
     __syncthreads();
     if (tid == 0) st_release(&J.flags[c], (unsigned)e);
   };
@@ -233,17 +339,27 @@ __global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) 
     }
     __syncthreads();
     if (bail) return false;
-    if (c > 0) {  // rows [r0-K, r0) = the lower neighbour's last K rows
-      const float *hn = J.halo + ((size_t)(e & 1) * G + (c - 1)) * 2 * K * P + K * P;
-      for (int r = 0; r < K; ++r)
-        for (int i = tid; i < nnx; i += kJBlock) D[(o0 - K + r) * P + i] = __ldcg(hn + r * P + i);
-    }
-    if (c < G - 1) {  // rows [r1, r1+K) = the upper neighbour's first K rows
-      const float *hn = J.halo + ((size_t)(e & 1) * G + (c + 1)) * 2 * K * P;
-      for (int r = 0; r < K; ++r)
-        for (int i = tid; i < nnx; i += kJBlock) D[(o1 + r) * P + i] = __ldcg(hn + r * P + i);
+    const float *hlo = J.halo + ((size_t)(e & 1) * G + (c - 1)) * 2 * K * P + K * P;
+    const float *hhi = J.halo + ((size_t)(e & 1) * G + (c + 1)) * 2 * K * P;
+    for (int i = tid; i < nnx; i += kJBlock) {
+      float vl[kMaxDepth], vh[kMaxDepth];
+#pragma unroll
+      for (int r = 0; r < kMaxDepth; ++r) {
+        vl[r] = (r < K && c > 0) ? __ldcg(hlo + r * P + i) : 0.0f;
+        vh[r] = (r < K && c < G - 1) ? __ldcg(hhi + r * P + i) : 0.0f;
+      }
+#pragma unroll
+      for (int r = 0; r < kMaxDepth; ++r) {
+        if (r < K && c > 0) D[(o0 - K + r) * P + i] = vl[r];  // the lower neighbour's last K rows
+        if (r < K && c < G - 1) D[(o1 + r) * P + i] = vh[r];  // the upper neighbour's first K rows
+      }
     }
     __syncthreads();
+    if constexpr (R > 0) {  // the strips' halo rows are new: reload the registers
+#pragma unroll
+      for (int r = 0; r < R; ++r)
+        if (r < rg.nvalid) x[r] = lds4(D + (rg.lr0 + r) * P + rg.col);
+    }
     return true;
   };
 
@@ -258,7 +374,13 @@ __global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) 
     const int u0 = max(1, r0 - K + m) - lo;          // updated local rows [u0, u1)
     const int u1 = min(nny - 2, r1 - 1 + K - m) + 1 - lo;
     float md;
-    if (pending) {
+    if (R > 0) {
+      if (pending) {
+        if (!receive(S, pending)) break;
+        pending = 0;
+      }
+      md = sweep(S, D, u0, u1, check);
+    } else if (pending) {
       // rows o0+1 .. o1-2 read only owned rows of S: sweep them first
       const int i0 = max(u0, o0 + 1), i1 = min(u1, o1 - 1);
       md = sweep(S, D, i0, i1, check);
@@ -332,6 +454,33 @@ __global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) 
     ctl->sweeps = done;
     ctl->residual = last;
   }
+}
+
+__global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) {
+  extern __shared__ __align__(16) float jsm[];
+  __shared__ float red[33];
+  __shared__ int bail;
+  if (threadIdx.x == 0) bail = 0;
+  __syncthreads();
+  switch (J.strip) {
+    case 1: jacobi_body<1>(a, J, jsm, red, &bail); break;
+    case 2: jacobi_body<2>(a, J, jsm, red, &bail); break;
+    case 4: jacobi_body<4>(a, J, jsm, red, &bail); break;
+    case 8: jacobi_body<8>(a, J, jsm, red, &bail); break;
+    default: jacobi_body<0>(a, J, jsm, red, &bail); break;
+  }
+}
+
+// strip height for the register-strip sweep: the smallest R in {1,2,4,8}
+// whose strips cover `urows` updatable rows of (nnx-1)/4 column groups with
+// one thread each; 0 (shared-memory sweep) when none does
+int jacobi_strip_rows(int nnx, int urows) {
+  if ((nnx - 1) % 4 != 0) return 0;
+  const int ng = (nnx - 1) / 4;
+  if (ng > kJBlock) return 0;
+  for (int r = 1; r <= 8; r *= 2)
+    if ((long long)ng * ((urows + r - 1) / r) <= kJBlock) return r;
+  return 0;
 }
 
 size_t jacobi_smem_bytes(int rows_per_cta, int depth, int pitch) {

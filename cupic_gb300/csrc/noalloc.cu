@@ -146,6 +146,7 @@ extern "C" int cupic_poisson_solver_static(const cupic_params *p, const int64_t 
   J.depth = K;
   J.pitch = P;
   J.vec = ((nnx - 1) % 4 == 0) ? 1 : 0;
+  J.strip = jacobi_strip_rows(nnx, B + 2 * (G > 1 ? K : 1) - 2);
   J.do_field = e_dev ? 1 : 0;
   J.write_stats = 1;
   J.flags = flags;
