@@ -188,16 +188,21 @@ int plan_jacobi(cupic_ctx *c) {
   const char *envk = getenv("CUPIC_JACOBI_DEPTH");
   int G = env ? atoi(env) : 0;
   int K = envk ? atoi(envk) : 0;
+  // A single CTA needs no inter-CTA traffic at all; it wins whenever the
+  // mesh fits and is small, or when convergence is checked often (every
+  // check of a multi-CTA solve is a grid barrier).
   if (G <= 0) {
-    if (M + 2 <= rows_fit && (long long)M * nnx <= 65536)
+    const bool fits = M + 2 <= rows_fit;
+    const bool frequent_checks = c->p.check_every < 16 && c->p.max_sweeps > c->p.min_sweeps;
+    if (fits && ((long long)M * nnx <= 65536 || frequent_checks))
       G = 1;
     else
       G = std::min(c->num_sms, M);
   }
   G = std::max(1, std::min(G, M));
   int B = (M + G - 1) / G;
-  if (K <= 0) K = 8;
-  K = std::max(1, std::min(K, M / G));
+  if (K <= 0) K = 16;
+  K = std::max(1, std::min(K, std::min(M / G, 16)));
   if (G == 1) K = 1;
   while (G > 1 && B + 2 * K > rows_fit) {  // shrink the depth, then add CTAs
     if (K > 1) {

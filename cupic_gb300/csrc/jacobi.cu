@@ -21,7 +21,6 @@ namespace cupic {
 namespace {
 
 constexpr int kJBlock = 512;
-constexpr int kMaxDepth = 8;  // largest temporal-blocking depth
 constexpr long long kSpinLimit = 1ll << 22;
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
@@ -319,12 +318,9 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
   auto publish = [&](const float *D, int e) {
     float *hp = J.halo + ((size_t)(e & 1) * G + c) * 2 * K * P;
     for (int i = tid; i < nnx; i += kJBlock) {
-#pragma unroll
-      for (int r = 0; r < kMaxDepth; ++r) {
-        if (r < K) {
-          __stcg(hp + r * P + i, D[(o0 + r) * P + i]);
-          __stcg(hp + (K + r) * P + i, D[(o1 - K + r) * P + i]);
-        }
+      for (int r = 0; r < K; ++r) {
+        __stcg(hp + r * P + i, D[(o0 + r) * P + i]);
+        __stcg(hp + (K + r) * P + i, D[(o1 - K + r) * P + i]);
       }
     }
     __syncthreads();
@@ -342,16 +338,20 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
     const float *hlo = J.halo + ((size_t)(e & 1) * G + (c - 1)) * 2 * K * P + K * P;
     const float *hhi = J.halo + ((size_t)(e & 1) * G + (c + 1)) * 2 * K * P;
     for (int i = tid; i < nnx; i += kJBlock) {
-      float vl[kMaxDepth], vh[kMaxDepth];
+      for (int rb = 0; rb < K; rb += 8) {  // batches of 8 rows: loads first, then stores
+        float vl[8], vh[8];
 #pragma unroll
-      for (int r = 0; r < kMaxDepth; ++r) {
-        vl[r] = (r < K && c > 0) ? __ldcg(hlo + r * P + i) : 0.0f;
-        vh[r] = (r < K && c < G - 1) ? __ldcg(hhi + r * P + i) : 0.0f;
-      }
+        for (int q = 0; q < 8; ++q) {
+          const int r = rb + q;
+          vl[q] = (r < K && c > 0) ? __ldcg(hlo + r * P + i) : 0.0f;
+          vh[q] = (r < K && c < G - 1) ? __ldcg(hhi + r * P + i) : 0.0f;
+        }
 #pragma unroll
-      for (int r = 0; r < kMaxDepth; ++r) {
-        if (r < K && c > 0) D[(o0 - K + r) * P + i] = vl[r];  // the lower neighbour's last K rows
-        if (r < K && c < G - 1) D[(o1 + r) * P + i] = vh[r];  // the upper neighbour's first K rows
+        for (int q = 0; q < 8; ++q) {
+          const int r = rb + q;
+          if (r < K && c > 0) D[(o0 - K + r) * P + i] = vl[q];  // the lower neighbour's last K rows
+          if (r < K && c < G - 1) D[(o1 + r) * P + i] = vh[q];  // the upper neighbour's first K rows
+        }
       }
     }
     __syncthreads();

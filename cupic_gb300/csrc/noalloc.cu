@@ -92,7 +92,7 @@ extern "C" int cupic_poisson_solver_static(const cupic_params *p, const int64_t 
   };
   // one CTA when the whole mesh fits; otherwise the most CTAs (up to one per
   // SM) for which some halo depth K >= 1 fits both the CTA's shared memory
-  // and the static scratch, with the deepest such K (at most 8)
+  // and the static scratch, with the deepest such K (at most 16)
   const char *env = getenv("CUPIC_JACOBI_CTAS");
   const int forced = env ? atoi(env) : 0;
   int G = 0, B = 0, K = 0;
@@ -104,7 +104,7 @@ extern "C" int cupic_poisson_solver_static(const cupic_params *p, const int64_t 
     const int gmax = std::max(1, std::min(forced > 0 ? forced : num_sms, M));
     for (int g = gmax; g >= 1 && K < 1; --g) {
       const int b = (M + g - 1) / g;
-      int k = g > 1 ? (int)std::min<long long>({8LL, (long long)(M / g), (rows_fit - b) / 2}) : 1;
+      int k = g > 1 ? (int)std::min<long long>({16LL, (long long)(M / g), (rows_fit - b) / 2}) : 1;
       while (k >= 1 && (need(g, k) > kStaticScratchBytes || b + 2 * k > rows_fit)) --k;
       if (k >= 1) {
         G = g;
