@@ -15,7 +15,9 @@ import numpy as np
 from .params import Params, StepStats, workload_params
 
 __all__ = ["Sim", "Params", "StepStats", "workload_params", "load_library", "library_path",
-           "CupicError", "params_from_input_data", "SPECIES", "FLAGS", "EXPORTED"]
+           "CupicError", "params_from_input_data", "SPECIES", "FLAGS", "EXPORTED",
+           "write_particles_file", "read_particles_file", "write_mesh_file",
+           "write_bookmarks_file", "write_bins_file", "rewrite_input_data", "driver_path"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
@@ -34,6 +36,10 @@ EXPORTED = [
     "cupic_get_bookmarks", "cupic_get_rho", "cupic_get_rho_fixed", "cupic_get_phi",
     "cupic_set_phi", "cupic_get_field", "cupic_get_phi_f32", "cupic_get_field_f32",
     "cupic_get_stats", "cupic_get_flags", "cupic_clear_flags", "cupic_poisson_solver_static",
+    "cupic_init_mesh", "cupic_get_params", "cupic_write_particles_file",
+    "cupic_read_particles_file", "cupic_write_mesh_file", "cupic_write_bookmarks_file",
+    "cupic_write_bins_file", "cupic_rewrite_input_data", "cupic_particles_snapshot",
+    "cupic_mesh_snapshot", "cupic_save_bm", "cupic_save_bins", "cupic_load_particles_file",
 ]
 
 
@@ -45,6 +51,11 @@ class CupicError(RuntimeError):
 
 def library_path():
     return os.path.join(_HERE, "_build", "libcupic_gpu.so")
+
+
+def driver_path():
+    """The drop-in program (the reference's main, src/main.cu:26-117)."""
+    return os.path.join(_HERE, "_build", "cupic_run")
 
 
 def load_library(build_if_missing=False):
@@ -97,6 +108,19 @@ def load_library(build_if_missing=False):
         "cupic_poisson_solver_static": [P(Params), ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_void_p, c_d, c_i32, c_i32, c_i32,
                                         ctypes.c_void_p, P(c_i32), P(ctypes.c_float)],
+        "cupic_init_mesh": [vp],
+        "cupic_get_params": [vp, P(Params)],
+        "cupic_write_particles_file": [ctypes.c_char_p, P(c_d), c_i64, ctypes.c_char_p],
+        "cupic_read_particles_file": [ctypes.c_char_p, P(c_d), c_i64, P(c_i64)],
+        "cupic_write_mesh_file": [ctypes.c_char_p, P(c_d), c_i32, c_i32],
+        "cupic_write_bookmarks_file": [ctypes.c_char_p, P(c_i32), c_i32],
+        "cupic_write_bins_file": [ctypes.c_char_p, P(c_d), c_i64, c_d],
+        "cupic_rewrite_input_data": [ctypes.c_char_p, c_i32],
+        "cupic_particles_snapshot": [vp, c_i, ctypes.c_char_p],
+        "cupic_mesh_snapshot": [vp, c_i, ctypes.c_char_p],
+        "cupic_save_bm": [vp, c_i, ctypes.c_char_p],
+        "cupic_save_bins": [vp, c_i, ctypes.c_char_p],
+        "cupic_load_particles_file": [vp, c_i, ctypes.c_char_p],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -122,6 +146,52 @@ def _ok(rc, what):
 
 def _ptr(a, ct):
     return a.ctypes.data_as(ctypes.POINTER(ct))
+
+
+def write_particles_file(path, xyvv, header=None):
+    """particles_snapshot's format (diagnostic.cu:76-79); `header` adds one
+    "# ..." line first."""
+    a = np.ascontiguousarray(xyvv, dtype=np.float64).reshape(-1, 4)
+    _ok(load_library().cupic_write_particles_file(
+        os.fsencode(path), _ptr(a, ctypes.c_double), a.shape[0],
+        None if header is None else header.encode()), "write_particles_file")
+
+
+def read_particles_file(path):
+    """Every line holding four numbers, as an (n, 4) float64 array."""
+    L = load_library()
+    n = ctypes.c_int64()
+    _ok(L.cupic_read_particles_file(os.fsencode(path), None, 0, ctypes.byref(n)),
+        "read_particles_file")
+    out = np.empty((max(n.value, 1), 4))
+    got = ctypes.c_int64()
+    _ok(L.cupic_read_particles_file(os.fsencode(path), _ptr(out, ctypes.c_double), n.value,
+                                    ctypes.byref(got)), "read_particles_file")
+    return out[:got.value]
+
+
+def write_mesh_file(path, m):
+    """mesh_snapshot's format (diagnostic.cu:118-125); m is (nny, nnx)."""
+    a = np.ascontiguousarray(m, dtype=np.float64)
+    _ok(load_library().cupic_write_mesh_file(os.fsencode(path), _ptr(a, ctypes.c_double),
+                                             a.shape[1], a.shape[0]), "write_mesh_file")
+
+
+def write_bookmarks_file(path, bm):
+    a = np.ascontiguousarray(bm, dtype=np.int32).ravel()
+    _ok(load_library().cupic_write_bookmarks_file(os.fsencode(path), _ptr(a, ctypes.c_int32),
+                                                  a.size // 2), "write_bookmarks_file")
+
+
+def write_bins_file(path, xyvv, ds):
+    a = np.ascontiguousarray(xyvv, dtype=np.float64).reshape(-1, 4)
+    _ok(load_library().cupic_write_bins_file(os.fsencode(path), _ptr(a, ctypes.c_double),
+                                             a.shape[0], ds), "write_bins_file")
+
+
+def rewrite_input_data(path, n_ini):
+    """main.cu:98-113: line 1 of input_data becomes "n_ini = <n_ini>;"."""
+    _ok(load_library().cupic_rewrite_input_data(os.fsencode(path), n_ini), "rewrite_input_data")
 
 
 def params_from_input_data(path):
@@ -171,6 +241,15 @@ class Sim:
         a = np.ascontiguousarray(xyvv, dtype=np.float64).reshape(-1, 4)
         _ok(self.L.cupic_load_particles(self.h, species, _ptr(a, ctypes.c_double), a.shape[0]),
             "load_particles")
+
+    def init_mesh(self):
+        """initialize_mesh after a load (init.cu:84-93): linear phi, deposit,
+        initial solve and field, clock at step n_ini+1."""
+        _ok(self.L.cupic_init_mesh(self.h), "init_mesh")
+
+    def load_file(self, species, path):
+        _ok(self.L.cupic_load_particles_file(self.h, species, os.fsencode(path)),
+            "load_particles_file")
 
     def set_time(self, step, t, tin_e=-1.0, tin_i=-1.0):
         _ok(self.L.cupic_set_time(self.h, step, t, tin_e, tin_i), "set_time")
@@ -286,3 +365,20 @@ class Sim:
 
     def clear_flags(self):
         _ok(self.L.cupic_clear_flags(self.h), "clear_flags")
+
+    # ---- the reference's files ---------------------------------------------
+    MESH = {"rho": 0, "rho_last": 1, "phi": 2, "ex": 3, "ey": 4}
+
+    def particles_snapshot(self, species, path):
+        _ok(self.L.cupic_particles_snapshot(self.h, species, os.fsencode(path)),
+            "particles_snapshot")
+
+    def mesh_snapshot(self, what, path):
+        w = self.MESH[what] if isinstance(what, str) else what
+        _ok(self.L.cupic_mesh_snapshot(self.h, w, os.fsencode(path)), "mesh_snapshot")
+
+    def save_bm(self, species, path):
+        _ok(self.L.cupic_save_bm(self.h, species, os.fsencode(path)), "save_bm")
+
+    def save_bins(self, species, path):
+        _ok(self.L.cupic_save_bins(self.h, species, os.fsencode(path)), "save_bins")

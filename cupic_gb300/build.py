@@ -16,7 +16,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcupic_gpu.so")
-SOURCES = ["capi.cu", "particles.cu", "jacobi.cu", "io.cu", "noalloc.cu"]
+EXE = os.path.join(OUT, "cupic_run")
+SOURCES = ["capi.cu", "particles.cu", "jacobi.cu", "io.cu", "noalloc.cu", "files.cpp"]
+MAIN = "cupic_main.cpp"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -65,7 +67,7 @@ def build(force=False, verbose=False):
     procs, objs = [], []
     for src in SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(OUT, src.replace(".cu", ".o"))
+        o = os.path.join(OUT, os.path.splitext(src)[0] + ".o")
         objs.append(o)
         if force or _stale(o, [s] + headers):
             cmd = [cc] + common_flags() + ["-c", s, "-o", o]
@@ -83,6 +85,12 @@ def build(force=False, verbose=False):
         raise RuntimeError(f"nvcc failed for {failed}")
     if force or procs or _stale(LIB, objs):
         cmd = [cc] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs
+        subprocess.run(cmd, check=True)
+    main = os.path.join(CSRC, MAIN)
+    if force or _stale(EXE, [main, LIB] + headers):
+        # the drop-in program: host code only, linked against the library
+        cmd = [shutil.which("g++") or "g++", "-O2", "-std=c++17", "-I", os.path.join(HERE, "..", "include"),
+               main, "-o", EXE, "-L", OUT, "-lcupic_gpu", "-Wl,-rpath,$ORIGIN"]
         subprocess.run(cmd, check=True)
     return LIB
 

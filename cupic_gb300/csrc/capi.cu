@@ -626,6 +626,31 @@ int cupic_init_plasma(cupic_ctx *c) {
   return finish(c);
 }
 
+int cupic_init_mesh(cupic_ctx *c) {
+  if (!c) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  CU(cudaStreamSynchronize(c->stream));
+  int rc = set_linear_phi(c);
+  if (rc) return rc;
+  rc = deposit_current(c);
+  if (rc) return rc;
+  const cupic_params &p = c->p;
+  CU(launch_jacobi(c->a, jargs(c, p.init_tol, p.init_min_sweeps, p.init_max_sweeps, p.check_every, 1),
+                   c->stream));
+  rc = sync_check(c);
+  if (rc) return rc;
+  rc = cupic_set_time(c, (int64_t)p.n_ini + 1, p.n_ini * p.dt + p.dt, -1.0, -1.0);
+  if (rc) return rc;
+  c->initialized = true;
+  return finish(c);
+}
+
+int cupic_get_params(cupic_ctx *c, cupic_params *p) {
+  if (!c || !p) return CUPIC_ERR_ARG;
+  *p = c->p;
+  return CUPIC_OK;
+}
+
 int cupic_load_particles(cupic_ctx *c, int sp, const double *xyvv, int64_t n) {
   if (!c || sp < 0 || sp > 1 || n < 0 || (n > 0 && !xyvv)) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));

@@ -147,6 +147,14 @@ int cupic_load_particles(struct cupic_ctx *ctx, int species, const double *xyvv,
 int cupic_set_time(struct cupic_ctx *ctx, int64_t step, double t, double tin_e, double tin_i);
 int cupic_get_time(struct cupic_ctx *ctx, int64_t *step, double *t, double *tin_e, double *tin_i);
 
+/* init_sim for n_ini > 0 after the particles were loaded: initialize_mesh
+ * (init.cu:202-260) -- linear phi, deposit, the initial solve (init_tol)
+ * and field, no leapfrog half-step -- then the clock set to step n_ini+1 at
+ * t = n_ini*dt + dt with the injection clocks unset (init.cu:86-93). */
+int cupic_init_mesh(struct cupic_ctx *ctx);
+/* The parameters the context was created with. */
+int cupic_get_params(struct cupic_ctx *ctx, cupic_params *p);
+
 /* ---- the cycle (reference entry points) -------------------------------- */
 
 /* Deposits rho from the current particles (only needed after a load). */
@@ -236,6 +244,42 @@ int cupic_poisson_solver_static(const cupic_params *p, const int64_t *rho_dev, f
                                 float *e_dev, double max_error, int32_t min_sweeps,
                                 int32_t max_sweeps, int32_t check_every, void *stream,
                                 int32_t *sweeps_out, float *residual_out);
+
+/* ---- the reference's text files ---------------------------------------- */
+/* Host-side only; paths are used as given (the reference's ".dat" suffix
+ * and "../output/" prefix are the caller's).  The formats are the
+ * reference's, character for character. */
+
+/* particles_snapshot (diagnostic.cu:48-87): " %.17e %.17e %.17e %.17e \n"
+ * per particle.  header != NULL first writes one line "# <header>", which
+ * the reference's loader skips as its header line (D12, init.cu:372). */
+int cupic_write_particles_file(const char *path, const double *xyvv, int64_t n,
+                               const char *header);
+/* read_particle_file (init.cu:348-420): every line holding four numbers is a
+ * particle, in file order; other lines (a header, blank lines) are skipped.
+ * Unlike the reference, the first particle of a header-less file is kept
+ * (defect D12 fixed).  xyvv == NULL only counts into *n_out. */
+int cupic_read_particles_file(const char *path, double *xyvv, int64_t capacity, int64_t *n_out);
+/* mesh_snapshot (diagnostic.cu:91-133): " %d %d %.17e \n", i outer, j
+ * inner, a blank line after each i; m is nnx*nny doubles, index i + j*nnx. */
+int cupic_write_mesh_file(const char *path, const double *m, int32_t nnx, int32_t nny);
+/* save_bm (diagnostic.cu:137-169): " %d %d %d \n" per cell row. */
+int cupic_write_bookmarks_file(const char *path, const int32_t *bm, int32_t ncy);
+/* save_bins (diagnostic.cu:173-215): " %d %d \n", index and int(y/ds). */
+int cupic_write_bins_file(const char *path, const double *xyvv, int64_t n, double ds);
+/* main.cu:98-113: line 1 of input_data becomes "n_ini = <n_ini>;", the
+ * other lines are kept (a last line without '\n' is kept too). */
+int cupic_rewrite_input_data(const char *path, int32_t n_ini);
+
+/* The same files straight from a context. */
+int cupic_particles_snapshot(struct cupic_ctx *ctx, int species, const char *path);
+/* what: 0 the charge the next solve uses, 1 the charge of the last solve
+ * (the reference's d_rho after a step), 2 phi, 3 Ex, 4 Ey */
+int cupic_mesh_snapshot(struct cupic_ctx *ctx, int what, const char *path);
+int cupic_save_bm(struct cupic_ctx *ctx, int species, const char *path);
+int cupic_save_bins(struct cupic_ctx *ctx, int species, const char *path);
+/* load_particles (init.cu:327-344) for one species from a particle file. */
+int cupic_load_particles_file(struct cupic_ctx *ctx, int species, const char *path);
 
 #ifdef __cplusplus
 }

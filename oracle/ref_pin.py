@@ -1,4 +1,6 @@
-"""Build and run the reference's own input_data getters (src/init.cu:424-789).
+"""Build and run the reference's own input_data getters (src/init.cu:424-789)
+and, in a second program, its particle-file reader and snapshot writers
+(src/init.cu:348-420, src/diagnostic.cu:48-215).
 
 TEST INFRASTRUCTURE ONLY.  The reference's sources are compiled where they
 lie (REF_SRC below) with nvcc into oracle/_ref/ -- never copied -- together with:
@@ -66,3 +68,45 @@ def run(input_text):
             f.write(input_text)
         out = subprocess.run([exe, d], capture_output=True, text=True, check=True).stdout
     return json.loads(out)
+
+
+FILES_BIN = os.path.join(OUT, "ref_files")
+
+
+def build_files(force=False):
+    """Compile oracle/_ref/ref_files: the reference's particle-file reader and
+    snapshot writers (init.cu, diagnostic.cu) with their cudaMalloc/cudaMemcpy
+    on host memory (ref_pin/host_mem.h), driven by ref_pin/files_main.cpp."""
+    if not available():
+        return None
+    if os.path.exists(FILES_BIN) and not force:
+        return FILES_BIN
+    build()
+    obj = os.path.join(OUT, "obj")
+    flags = ["-gencode", "arch=compute_103a,code=sm_103a", "-dc", "-I", PIN, "-w",
+             "-include", os.path.join(PIN, "host_mem.h")]
+    procs = [subprocess.Popen(["nvcc"] + flags + [os.path.join(REF_SRC, u + ".cu"), "-o",
+                                                  os.path.join(obj, u + "_host.o")])
+             for u in ("init", "diagnostic")]
+    for p in procs:
+        if p.wait() != 0:
+            raise RuntimeError("nvcc failed on a reference source")
+    subprocess.run(["g++", "-O0", "-c", os.path.join(PIN, "files_main.cpp"), "-o",
+                    os.path.join(obj, "files_main.o")], check=True)
+    objs = [os.path.join(obj, n + ".o") for n in
+            ("init_host", "diagnostic_host", "cc", "particles", "cuda", "mesh", "gsl_shim",
+             "files_main")]
+    subprocess.run(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a"] + objs +
+                   ["-o", FILES_BIN], check=True)
+    return FILES_BIN
+
+
+def run_files(workdir):
+    """Runs ref_files in workdir (input/ prepared by the caller); the
+    reference's files appear in workdir/output."""
+    exe = build_files()
+    if exe is None:
+        raise RuntimeError("reference sources not available")
+    os.makedirs(os.path.join(workdir, "run"), exist_ok=True)
+    os.makedirs(os.path.join(workdir, "output"), exist_ok=True)
+    subprocess.run([exe, workdir], check=True)
