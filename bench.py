@@ -385,7 +385,8 @@ def run_cupic(args, world, rank, local):
                        "l2": "inputs larger than L2 (particle arrays 3.4 GB); the 4 MB mesh "
                              "stays L2/shared-memory resident by design",
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "jacobi_ctas": None},
+                       "jacobi_plan": dict(zip(("ctas", "rows_per_cta", "halo_depth"),
+                                               sim.solver_plan()))},
             "e2e": e2e,
             "gpu_launches": KERNELS_PER_STEP * args.steps,
             "roofline": dominant,

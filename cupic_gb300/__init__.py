@@ -36,7 +36,7 @@ EXPORTED = [
     "cupic_get_bookmarks", "cupic_get_rho", "cupic_get_rho_fixed", "cupic_get_phi",
     "cupic_set_phi", "cupic_get_field", "cupic_get_phi_f32", "cupic_get_field_f32",
     "cupic_get_stats", "cupic_get_flags", "cupic_clear_flags", "cupic_poisson_solver_static",
-    "cupic_init_mesh", "cupic_get_params", "cupic_write_particles_file",
+    "cupic_init_mesh", "cupic_get_params", "cupic_get_solver_plan", "cupic_write_particles_file",
     "cupic_read_particles_file", "cupic_write_mesh_file", "cupic_write_bookmarks_file",
     "cupic_write_bins_file", "cupic_rewrite_input_data", "cupic_particles_snapshot",
     "cupic_mesh_snapshot", "cupic_save_bm", "cupic_save_bins", "cupic_load_particles_file",
@@ -110,6 +110,7 @@ def load_library(build_if_missing=False):
                                         ctypes.c_void_p, P(c_i32), P(ctypes.c_float)],
         "cupic_init_mesh": [vp],
         "cupic_get_params": [vp, P(Params)],
+        "cupic_get_solver_plan": [vp, P(c_i32), P(c_i32), P(c_i32)],
         "cupic_write_particles_file": [ctypes.c_char_p, P(c_d), c_i64, ctypes.c_char_p],
         "cupic_read_particles_file": [ctypes.c_char_p, P(c_d), c_i64, P(c_i64)],
         "cupic_write_mesh_file": [ctypes.c_char_p, P(c_d), c_i32, c_i32],
@@ -246,6 +247,13 @@ class Sim:
         """initialize_mesh after a load (init.cu:84-93): linear phi, deposit,
         initial solve and field, clock at step n_ini+1."""
         _ok(self.L.cupic_init_mesh(self.h), "init_mesh")
+
+    def solver_plan(self):
+        """(CTAs, rows per CTA, halo depth) of the Jacobi solver."""
+        g, b, k = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _ok(self.L.cupic_get_solver_plan(self.h, ctypes.byref(g), ctypes.byref(b), ctypes.byref(k)),
+            "get_solver_plan")
+        return g.value, b.value, k.value
 
     def load_file(self, species, path):
         _ok(self.L.cupic_load_particles_file(self.h, species, os.fsencode(path)),

@@ -17,8 +17,10 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcupic_gpu.so")
 EXE = os.path.join(OUT, "cupic_run")
+REF_LIB = os.path.join(OUT, "libcupic_ref.so")
 SOURCES = ["capi.cu", "particles.cu", "jacobi.cu", "io.cu", "noalloc.cu", "files.cpp"]
 MAIN = "cupic_main.cpp"
+REF_API = "ref_api.cpp"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -86,12 +88,17 @@ def build(force=False, verbose=False):
     if force or procs or _stale(LIB, objs):
         cmd = [cc] + ARCH + ["-shared", "-cudart", "static", "-o", LIB] + objs
         subprocess.run(cmd, check=True)
+    gxx = [shutil.which("g++") or "g++", "-O2", "-std=c++17", "-I", os.path.join(HERE, "..", "include")]
+    link = ["-L", OUT, "-lcupic_gpu", "-Wl,-rpath,$ORIGIN"]
+    headers.append(os.path.join(HERE, "..", "include", "cupic_ref.h"))
     main = os.path.join(CSRC, MAIN)
     if force or _stale(EXE, [main, LIB] + headers):
         # the drop-in program: host code only, linked against the library
-        cmd = [shutil.which("g++") or "g++", "-O2", "-std=c++17", "-I", os.path.join(HERE, "..", "include"),
-               main, "-o", EXE, "-L", OUT, "-lcupic_gpu", "-Wl,-rpath,$ORIGIN"]
-        subprocess.run(cmd, check=True)
+        subprocess.run(gxx + [main, "-o", EXE] + link, check=True)
+    ref = os.path.join(CSRC, REF_API)
+    if force or _stale(REF_LIB, [ref, LIB] + headers):
+        # the reference's C++ host functions over the C-ABI
+        subprocess.run(gxx + ["-shared", "-fPIC", ref, "-o", REF_LIB] + link, check=True)
     return LIB
 
 

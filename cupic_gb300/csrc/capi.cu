@@ -10,7 +10,10 @@
 #include <string.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <new>
+#include <tuple>
 #include <vector>
 
 #include "cupic_internal.cuh"
@@ -23,6 +26,9 @@ struct cupic_ctx {
   int device = 0;
   int num_sms = 0;
   cudaStream_t stream = nullptr;
+  // side branch of a step: the injection draws run beside the push
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   SimArgs a{};
   Ctl *ctl = nullptr;
   std::vector<int64_t> seg[2];
@@ -173,24 +179,69 @@ void fill_constants(cupic_ctx *c) {
   a.k1 = (uint32_t)(p.seed >> 32);
 }
 
-// Jacobi geometry: G CTAs of 1024 threads, each holding its rows (+ halos)
-// in shared memory.  Small meshes run in one CTA (no inter-CTA traffic at
-// all); larger ones spread over the SMs with temporal blocking depth K.
-// CUPIC_JACOBI_CTAS / CUPIC_JACOBI_DEPTH override the choice (tuning).
-int plan_jacobi(cupic_ctx *c) {
-  const int M = c->a.nny - 2, nnx = c->a.nnx;
-  int dev_max = 0;
-  CU(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
-  const int P = (nnx + 3) / 4 * 4;  // 16-byte aligned rows
+JacobiArgs jargs(const cupic_ctx *c, double tol, int mn, int mx, int chk, int field);
+
+// ---- Jacobi layout -------------------------------------------------------
+// G CTAs of 512 threads, each holding its B mesh rows plus K halo rows on
+// each side in shared memory; neighbours trade K rows every K sweeps.  The
+// layout changes only the speed: every plan computes the same bits.
+
+// Padded row pitch (16-byte rows) and the rows one CTA's shared memory holds.
+void jacobi_geometry(const cupic_ctx *c, int dev_max, int *P, long long *rows_fit) {
+  *P = (c->a.nnx + 3) / 4 * 4;
   const size_t avail = (size_t)dev_max - 1024;  // static shared memory of the kernel
-  const long long rows_fit = (long long)(avail / (3 * sizeof(float) * (size_t)P));
+  *rows_fit = (long long)(avail / (3 * sizeof(float) * (size_t)*P));
+}
+
+// Rows per CTA for G CTAs at depth K, or 0 if the layout does not fit.
+int jacobi_rows(const cupic_ctx *c, int G, int K, int P, long long rows_fit) {
+  const int M = c->a.nny - 2;
+  if (G < 1 || G > M || K < 1) return 0;
+  const int B = (M + G - 1) / G;
+  if (G > 1 && K > M / G) return 0;  // a CTA sends K of its own rows (it owns >= M/G)
+  if (B + 2 * (G > 1 ? K : 1) > rows_fit) return 0;
+  int per_sm = 0;
+  if (jacobi_set_smem(jacobi_smem_bytes(B, G > 1 ? K : 1, P)) != cudaSuccess ||
+      jacobi_max_ctas(jacobi_smem_bytes(B, G > 1 ? K : 1, P), &per_sm) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  if (per_sm < 1 || G > per_sm * c->num_sms) return 0;
+  return B;
+}
+
+int alloc_jacobi_scratch(cupic_ctx *c, int G, long long GK, int P) {
+  cudaFree(c->jflags);
+  cudaFree(c->jres);
+  cudaFree(c->jhalo);
+  c->jflags = nullptr;
+  c->jres = nullptr;
+  c->jhalo = nullptr;
+  CU(dalloc(&c->jflags, (size_t)G + 1));
+  CU(dalloc(&c->jres, (size_t)2 * G));
+  CU(dalloc(&c->jhalo, (size_t)4 * GK * P));
+  return CUPIC_OK;
+}
+
+int set_jacobi_plan(cupic_ctx *c, int G, int B, int K, int P) {
+  c->jG = G;
+  c->jB = B;
+  c->jK = G > 1 ? K : 1;
+  c->jP = P;
+  CU(jacobi_set_smem(jacobi_smem_bytes(B, c->jK, P)));
+  return alloc_jacobi_scratch(c, G, (long long)G * c->jK, P);
+}
+
+// The fixed rule, used when tuning is off or a layout is forced with
+// CUPIC_JACOBI_CTAS / CUPIC_JACOBI_DEPTH: one CTA for small meshes or
+// frequent convergence checks (each check of a multi-CTA solve is a grid
+// barrier), else one CTA per SM with the deepest halo that fits.
+int plan_jacobi_rule(cupic_ctx *c, int P, long long rows_fit) {
+  const int M = c->a.nny - 2, nnx = c->a.nnx;
   const char *env = getenv("CUPIC_JACOBI_CTAS");
   const char *envk = getenv("CUPIC_JACOBI_DEPTH");
   int G = env ? atoi(env) : 0;
   int K = envk ? atoi(envk) : 0;
-  // A single CTA needs no inter-CTA traffic at all; it wins whenever the
-  // mesh fits and is small, or when convergence is checked often (every
-  // check of a multi-CTA solve is a grid barrier).
   if (G <= 0) {
     const bool fits = M + 2 <= rows_fit;
     const bool frequent_checks = c->p.check_every < 16 && c->p.max_sweeps > c->p.min_sweeps;
@@ -213,19 +264,115 @@ int plan_jacobi(cupic_ctx *c) {
     }
   }
   if (B + 2 * K > rows_fit) return CUPIC_ERR_ARG;
-  const size_t sm = jacobi_smem_bytes(B, K, P);
-  CU(jacobi_set_smem(sm));
-  int per_sm = 0;
-  CU(jacobi_max_ctas(sm, &per_sm));
-  if (per_sm < 1 || G > per_sm * c->num_sms) return CUPIC_ERR_ARG;
-  c->jG = G;
-  c->jB = B;
-  c->jK = K;
-  c->jP = P;
-  CU(dalloc(&c->jflags, (size_t)G + 1));
-  CU(dalloc(&c->jres, (size_t)2 * G));
-  CU(dalloc(&c->jhalo, (size_t)2 * G * 2 * K * P));
-  return CUPIC_OK;
+  if (!jacobi_rows(c, G, K, P, rows_fit)) return CUPIC_ERR_ARG;
+  return set_jacobi_plan(c, G, B, K, P);
+}
+
+// Autotuner: times every feasible (CTAs, depth) layout on this context's own
+// buffers for the solve it will run (its check interval, up to 256 sweeps,
+// with the field) and keeps the fastest.  Results are cached per device and
+// mesh shape, so contexts of one shape tune once per process.
+struct TuneKey {
+  int device, nnx, nny, chk, sweeps;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(device, nnx, nny, chk, sweeps) < std::tie(o.device, o.nnx, o.nny, o.chk, o.sweeps);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, std::pair<int, int>> g_tuned;  // -> (G, K)
+
+int tune_jacobi(cupic_ctx *c, int P, long long rows_fit) {
+  const int M = c->a.nny - 2;
+  const int chk = std::max(1, c->p.check_every);
+  const int S = std::max(1, std::min(std::max(c->p.max_sweeps, c->p.init_max_sweeps), 256));
+  const TuneKey key{c->device, c->a.nnx, c->a.nny, chk, S};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      const int G = it->second.first, K = it->second.second;
+      const int B = jacobi_rows(c, G, K, P, rows_fit);
+      if (B) return set_jacobi_plan(c, G, B, K, P);
+    }
+  }
+  struct Cand { int G, B, K; };
+  std::vector<Cand> cands;
+  const int ns = c->num_sms;
+  const int gs[] = {1, 2, 4, 8, 16, 24, ns / 4, ns / 2, ns};
+  int maxG = 1;
+  long long maxGK = 1;
+  for (int G : gs) {
+    if (G < 1 || G > M) continue;
+    if (!cands.empty() && cands.back().G == G) continue;
+    // powers of two and the deepest halo that fits
+    int kmax = G == 1 ? 1 : std::min(16, M / G);
+    while (kmax > 1 && !jacobi_rows(c, G, kmax, P, rows_fit)) --kmax;
+    for (int K : {1, 2, 4, 8, 16, kmax}) {
+      if (K > kmax) continue;
+      if (!cands.empty() && cands.back().G == G && cands.back().K >= K) continue;
+      const int B = jacobi_rows(c, G, K, P, rows_fit);
+      if (!B) continue;
+      cands.push_back({G, B, K});
+      maxG = std::max(maxG, G);
+      maxGK = std::max(maxGK, (long long)G * K);
+    }
+  }
+  if (cands.empty()) return plan_jacobi_rule(c, P, rows_fit);
+  int rc = alloc_jacobi_scratch(c, maxG, maxGK, P);
+  if (rc) return rc;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  float best = 1e30f;
+  Cand pick = cands.front();
+  for (const Cand &cd : cands) {
+    c->jG = cd.G;
+    c->jB = cd.B;
+    c->jK = cd.G > 1 ? cd.K : 1;
+    c->jP = P;
+    JacobiArgs J = jargs(c, 0.0, S, S, chk, 1);
+    J.write_stats = 0;
+    float t = 1e30f;
+    bool ok = true;
+    for (int rep = 0; rep < 3 && ok; ++rep) {
+      ok = cudaEventRecord(e0, c->stream) == cudaSuccess &&
+           launch_jacobi(c->a, J, c->stream) == cudaSuccess &&
+           cudaEventRecord(e1, c->stream) == cudaSuccess &&
+           cudaEventSynchronize(e1) == cudaSuccess;
+      float ms = 0.0f;
+      if (ok && rep > 0 && cudaEventElapsedTime(&ms, e0, e1) == cudaSuccess) t = std::min(t, ms);
+    }
+    if (!ok) {
+      cudaGetLastError();
+      continue;
+    }
+    if (t < best) {
+      best = t;
+      pick = cd;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  // a solve that gave up waiting leaves a flag: clear what the trials raised
+  CU(cudaMemsetAsync(&c->ctl->step_flags, 0, sizeof(uint32_t), c->stream));
+  CU(cudaStreamSynchronize(c->stream));
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[key] = {pick.G, pick.K};
+  }
+  return set_jacobi_plan(c, pick.G, pick.B, pick.K, P);
+}
+
+int plan_jacobi(cupic_ctx *c) {
+  int dev_max = 0;
+  CU(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+  int P = 0;
+  long long rows_fit = 0;
+  jacobi_geometry(c, dev_max, &P, &rows_fit);
+  const char *tune = getenv("CUPIC_JACOBI_TUNE");
+  if (getenv("CUPIC_JACOBI_CTAS") || getenv("CUPIC_JACOBI_DEPTH") || (tune && atoi(tune) == 0))
+    return plan_jacobi_rule(c, P, rows_fit);
+  return tune_jacobi(c, P, rows_fit);
 }
 
 JacobiArgs jargs(const cupic_ctx *c, double tol, int mn, int mx, int chk, int field) {
@@ -300,13 +447,21 @@ int finish(cupic_ctx *c) {
   return flag_status(f);
 }
 
+// One step: solve + field, then the injection draws on the side stream while
+// the main stream clears the next charge, pushes and appends the movers;
+// the injected particles are appended once both branches are done.
 int enqueue_step(cupic_ctx *c) {
   const cupic_params &p = c->p;
   CU(launch_jacobi(c->a, jargs(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1), c->stream));
+  CU(cudaEventRecord(c->ev_fork, c->stream));
+  CU(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
+  CU(launch_inject_draw(c->a, c->side));
+  CU(cudaEventRecord(c->ev_join, c->side));
   CU(launch_zero_next_rho(c->a, c->stream));
   CU(launch_push_deposit(c->a, c->stream));
   CU(launch_arrive(c->a, c->stream));
-  CU(launch_inject(c->a, c->stream));
+  CU(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+  CU(launch_inject_append(c->a, c->stream));
   CU(launch_finalize(c->a, c->stream));
   return CUPIC_OK;
 }
@@ -523,7 +678,10 @@ int cupic_create(const cupic_params *pin, int device, cupic_ctx **out) {
   if (cudaSetDevice(device) != cudaSuccess) return fail(CUPIC_ERR_CUDA);
   if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
     return fail(CUPIC_ERR_CUDA);
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
     return fail(CUPIC_ERR_CUDA);
   fill_constants(c);
   SimArgs &a = c->a;
@@ -566,6 +724,10 @@ int cupic_destroy(cupic_ctx *c) {
   cudaFree(c->jflags);
   cudaFree(c->jres);
   cudaFree(c->jhalo);
+  if (c->side) cudaStreamSynchronize(c->side);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->ev_join) cudaEventDestroy(c->ev_join);
+  if (c->side) cudaStreamDestroy(c->side);
   if (c->stream) cudaStreamDestroy(c->stream);
   delete c;
   return CUPIC_OK;
@@ -651,6 +813,14 @@ int cupic_get_params(cupic_ctx *c, cupic_params *p) {
   return CUPIC_OK;
 }
 
+int cupic_get_solver_plan(cupic_ctx *c, int32_t *ctas, int32_t *rows_per_cta, int32_t *depth) {
+  if (!c) return CUPIC_ERR_ARG;
+  if (ctas) *ctas = c->jG;
+  if (rows_per_cta) *rows_per_cta = c->jB;
+  if (depth) *depth = c->jK;
+  return CUPIC_OK;
+}
+
 int cupic_load_particles(cupic_ctx *c, int sp, const double *xyvv, int64_t n) {
   if (!c || sp < 0 || sp > 1 || n < 0 || (n > 0 && !xyvv)) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
@@ -710,6 +880,9 @@ int cupic_load_particles(cupic_ctx *c, int sp, const double *xyvv, int64_t n) {
 int cupic_charge_deposition(cupic_ctx *c) {
   if (!c) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
+  // a step's push already deposited the moved and injected particles into
+  // the accumulator the next solve reads; the integer sums are identical
+  if (c->rho_valid) return sync_check(c);
   int rc = deposit_current(c);
   if (rc) return rc;
   return sync_check(c);
@@ -749,6 +922,7 @@ int cupic_particle_mover(cupic_ctx *c) {
   CU(launch_zero_next_rho(c->a, c->stream));
   CU(launch_push_deposit(c->a, c->stream));
   CU(launch_arrive(c->a, c->stream));
+  c->rho_valid = false;  // until cc completes the next charge
   return finish(c);
 }
 
@@ -849,16 +1023,24 @@ int cupic_step_timed(cupic_ctx *c, int32_t nsteps, float *phase_ms, int32_t npha
   const JacobiArgs J = jargs(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1);
   cudaError_t e = rc ? cudaErrorUnknown : cudaEventRecord(ev[0], c->stream);
   for (int s = 0; s < nsteps && e == cudaSuccess; ++s) {
+    // the launch order of enqueue_step, with an event after each
+    // main-stream kernel; the inject phase is the wait for the side branch
+    // (draws) plus the append
     cudaEvent_t *q = &ev[(size_t)s * per + 1];
     e = launch_jacobi(c->a, J, c->stream);
     if (e == cudaSuccess) e = cudaEventRecord(q[0], c->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev_fork, c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
+    if (e == cudaSuccess) e = launch_inject_draw(c->a, c->side);
+    if (e == cudaSuccess) e = cudaEventRecord(c->ev_join, c->side);
     if (e == cudaSuccess) e = launch_zero_next_rho(c->a, c->stream);
     if (e == cudaSuccess) e = cudaEventRecord(q[1], c->stream);
     if (e == cudaSuccess) e = launch_push_deposit(c->a, c->stream);
     if (e == cudaSuccess) e = cudaEventRecord(q[2], c->stream);
     if (e == cudaSuccess) e = launch_arrive(c->a, c->stream);
     if (e == cudaSuccess) e = cudaEventRecord(q[3], c->stream);
-    if (e == cudaSuccess) e = launch_inject(c->a, c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_join, 0);
+    if (e == cudaSuccess) e = launch_inject_append(c->a, c->stream);
     if (e == cudaSuccess) e = cudaEventRecord(q[4], c->stream);
     if (e == cudaSuccess) e = launch_finalize(c->a, c->stream);
     if (e == cudaSuccess) e = cudaEventRecord(q[5], c->stream);

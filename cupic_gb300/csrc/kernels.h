@@ -15,6 +15,8 @@ cudaError_t launch_leapfrog_start(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_push_deposit(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_arrive(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_inject(const SimArgs &a, cudaStream_t st);
+cudaError_t launch_inject_draw(const SimArgs &a, cudaStream_t st);
+cudaError_t launch_inject_append(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_finalize(const SimArgs &a, cudaStream_t st);
 size_t push_smem_bytes(int nnx);
 cudaError_t push_set_smem(size_t bytes);

@@ -252,6 +252,18 @@ constexpr int kPB = 512;       // threads
 constexpr int kPPT = 2;        // particles per thread per chunk
 constexpr int kStages = 3;     // chunks in flight
 constexpr int kCH = kPB * kPPT;
+// scan entries per chunk: one per (particle slot j, warp), 32 particles each
+constexpr int kNE = kPPT * (kPB / 32);
+static_assert(kNE <= 32, "one warp scans a chunk's entries");
+
+// three counts packed in 32 bits: 10 + 11 + 11 bits, enough for every
+// exclusive prefix of a chunk (at most 32*(kNE-1) = 992)
+__device__ __forceinline__ uint32_t pack3(int a, int b, int c) {
+  return (uint32_t)a | ((uint32_t)b << 10) | ((uint32_t)c << 21);
+}
+__device__ __forceinline__ uint32_t field0(uint32_t v) { return v & 0x3ffu; }
+__device__ __forceinline__ uint32_t field1(uint32_t v) { return (v >> 10) & 0x7ffu; }
+__device__ __forceinline__ uint32_t field2(uint32_t v) { return v >> 21; }
 }  // namespace
 
 size_t push_smem_bytes(int nnx) {
@@ -262,7 +274,7 @@ size_t push_smem_bytes(int nnx) {
 __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
   extern __shared__ __align__(128) unsigned char push_raw[];
   constexpr int NW = kPB / 32;
-  constexpr int NE = kPPT * NW;  // scan entries per chunk, (j, warp) in j-major order
+  constexpr int NE = kNE;  // scan entries per chunk, (j, warp) in j-major order
   const int s = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nnx = a.nnx;
   const int ncx = a.ncx;
@@ -271,9 +283,7 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
   long long *tnode = reinterpret_cast<long long *>(etile + 2 * ncx);  // node rows s-1..s+2
   int *tmom = reinterpret_cast<int *>(tnode + 4 * nnx);               // cell rows s-1..s+1
   __shared__ __align__(8) uint64_t full[kStages];
-  __shared__ unsigned long long wsum[NE];
-  __shared__ unsigned long long woff[NE];
-  __shared__ unsigned long long wtot;
+  __shared__ uint32_t wsum[2][NE];  // per-entry packed counts, alternate chunks
   __shared__ unsigned long long s_cnt[4];
 
   Ctl *ctl = a.ctl;
@@ -352,17 +362,15 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
       }
     }
     uint32_t bs[kPPT], bu[kPPT], bd[kPPT];
+    uint32_t *ws = wsum[k & 1];
 #pragma unroll
     for (int j = 0; j < kPPT; ++j) {
       bs[j] = __ballot_sync(kFull, cat[j] == 0);
       bu[j] = __ballot_sync(kFull, cat[j] == 1);
       bd[j] = __ballot_sync(kFull, cat[j] == 2);
-      if (lane == 0)
-        wsum[j * NW + warp] = (unsigned long long)__popc(bs[j]) |
-                              ((unsigned long long)__popc(bu[j]) << 21) |
-                              ((unsigned long long)__popc(bd[j]) << 42);
+      if (lane == 0) ws[j * NW + warp] = pack3(__popc(bs[j]), __popc(bu[j]), __popc(bd[j]));
     }
-    __syncthreads();
+    __syncthreads();  // the only block barrier of a chunk
     // every thread holds its particles: refill this stage with chunk k+kStages
     if (tid == 0 && k + kStages < nct) {
       const int k2 = k + kStages;
@@ -374,44 +382,39 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
       bulk_g2s(stage + st * kCH, (sp1 ? row1 : row0) + (size_t)q2 * kCH, (uint32_t)cnt2 * 16u,
                &full[st]);
     }
-    if (warp == 0) {
-      unsigned long long carry = 0ull;
+    // Every warp scans the chunk's NE entries itself (no second barrier).
+    // Exclusive prefixes are at most 32*(NE-1) < 1024 per field, so the
+    // packed sums never carry between fields; the chunk totals come from the
+    // last entry field by field.
+    const uint32_t v = lane < NE ? ws[lane] : 0u;
+    uint32_t inc = v;
 #pragma unroll
-      for (int b = 0; b < NE; b += 32) {
-        const unsigned long long v = (b + lane < NE) ? wsum[b + lane] : 0ull;
-        unsigned long long inc = v;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const unsigned long long u = __shfl_up_sync(kFull, inc, o);
-          if (lane >= o) inc += u;
-        }
-        if (b + lane < NE) woff[b + lane] = carry + inc - v;
-        carry += __shfl_sync(kFull, inc, 31);
-      }
-      if (lane == 0) wtot = carry;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(kFull, inc, o);
+      if (lane >= o) inc += u;
     }
-    __syncthreads();
+    const uint32_t ex = inc - v;
+    const uint32_t exl = __shfl_sync(kFull, ex, NE - 1), vl = __shfl_sync(kFull, v, NE - 1);
     float4 *sup = S.stage_up + (size_t)s * S.stage_cap;
     float4 *sdn = S.stage_down + (size_t)s * S.stage_cap;
     const int qc = sp == 0 ? -1 : 1;
 #pragma unroll
     for (int j = 0; j < kPPT; ++j) {
-      const unsigned long long off = woff[j * NW + warp];
+      const uint32_t off = __shfl_sync(kFull, ex, j * NW + warp);
       if (cat[j] == 0) {
-        row[c_stay + (int)(off & 0x1fffffull) + __popc(bs[j] & lt)] = p[j];
+        row[c_stay + (int)field0(off) + __popc(bs[j] & lt)] = p[j];
       } else if (cat[j] == 1) {
-        const int pos = c_up + (int)((off >> 21) & 0x1fffffull) + __popc(bu[j] & lt);
+        const int pos = c_up + (int)field1(off) + __popc(bu[j] & lt);
         if (pos < S.stage_cap) sup[pos] = p[j]; else fl |= CUPIC_FLAG_STAGE;
       } else if (cat[j] == 2) {
-        const int pos = c_dn + (int)((off >> 42) & 0x1fffffull) + __popc(bd[j] & lt);
+        const int pos = c_dn + (int)field2(off) + __popc(bd[j] & lt);
         if (pos < S.stage_cap) sdn[pos] = p[j]; else fl |= CUPIC_FLAG_STAGE;
       }
       if (cat[j] < 3) T.deposit(a, p[j].x, p[j].y, qc);
     }
-    const unsigned long long tot = wtot;
-    c_stay += (int)(tot & 0x1fffffull);
-    c_up += (int)((tot >> 21) & 0x1fffffull);
-    c_dn += (int)((tot >> 42) & 0x1fffffull);
+    c_stay += (int)(field0(exl) + field0(vl));
+    c_up += (int)(field1(exl) + field1(vl));
+    c_dn += (int)(field2(exl) + field2(vl));
     const bool last_of_species = (k == nct - 1) || (k == nc0 - 1);
     if (tid == 0 && last_of_species) {
       S.nstay[s] = c_stay;
@@ -698,16 +701,26 @@ cudaError_t launch_arrive(const SimArgs &a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_inject(const SimArgs &a, cudaStream_t st) {
+// The draws depend only on the clocks and the step's field, so a step can
+// run them beside the push; the append needs the push's row counts.
+cudaError_t launch_inject_draw(const SimArgs &a, cudaStream_t st) {
   const int cap = max(a.sp[0].inj_cap, a.sp[1].inj_cap);
   k_inject_sched<<<1, 32, 0, st>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_inject_gen<<<dim3((cap + 127) / 128, 2), 128, 0, st>>>(a);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_inject_append(const SimArgs &a, cudaStream_t st) {
   k_inject_append<<<2, kInjBlock, a.ncy * sizeof(int), st>>>(a);
   return cudaGetLastError();
+}
+
+cudaError_t launch_inject(const SimArgs &a, cudaStream_t st) {
+  cudaError_t e = launch_inject_draw(a, st);
+  if (e != cudaSuccess) return e;
+  return launch_inject_append(a, st);
 }
 
 cudaError_t launch_finalize(const SimArgs &a, cudaStream_t st) {

@@ -154,6 +154,10 @@ int cupic_get_time(struct cupic_ctx *ctx, int64_t *step, double *t, double *tin_
 int cupic_init_mesh(struct cupic_ctx *ctx);
 /* The parameters the context was created with. */
 int cupic_get_params(struct cupic_ctx *ctx, cupic_params *p);
+/* The Jacobi solver's layout: CTAs of the cooperative grid, mesh rows each
+ * CTA owns, and the halo depth (sweeps between neighbour exchanges). */
+int cupic_get_solver_plan(struct cupic_ctx *ctx, int32_t *ctas, int32_t *rows_per_cta,
+                          int32_t *depth);
 
 /* ---- the cycle (reference entry points) -------------------------------- */
 
@@ -182,7 +186,9 @@ enum {
   CUPIC_PHASE_ZERO = 1,   /* clearing the next charge accumulator (mesh.cu:35) */
   CUPIC_PHASE_PUSH = 2,   /* push + wrap + binning + deposition (particles.cu, cc.cu, mesh.cu) */
   CUPIC_PHASE_ARRIVE = 3, /* movers appended to their new rows (cc.cu:640-772) */
-  CUPIC_PHASE_INJECT = 4, /* injected flux (cc.cu:134-272) */
+  CUPIC_PHASE_INJECT = 4, /* injected flux (cc.cu:134-272): the draws run on a side stream
+                             beside the push; this phase is the wait for them plus the
+                             append of the injected particles */
   CUPIC_PHASE_FINAL = 5,  /* per-step counters and clock */
   CUPIC_NPHASE = 6
 };

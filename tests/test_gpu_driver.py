@@ -101,6 +101,7 @@ def test_restart_matches_oracle(first_run, tmp_path):
     r = run(tmp_path, "restart")
     text = (d / "input" / "input_data").read_text().replace("n_fin = 20;", "n_fin = 30;")
     (r / "input" / "input_data").write_text(text)
+    (r / "input_at_start").write_text(text)
     for s in ("electrons", "ions"):
         shutil.copy(d / "output" / "particles" / f"{s}_t_20.dat", r / "restart" / f"{s}.dat")
     out = drive(r)
@@ -110,7 +111,7 @@ def test_restart_matches_oracle(first_run, tmp_path):
     # every particle of the restart files is loaded (D12 fixed)
     for s in ("electrons", "ions"):
         np.testing.assert_array_equal(snap(r, s, 20), snap(d, s, 20))
-    p = cg.params_from_input_data(r / "input" / "input_data")
+    p = cg.params_from_input_data(r / "input_at_start")
     assert p.n_ini == 20
     ora = Oracle(p, fp64=False)
     ora.load(0, snap(d, "electrons", 20))
@@ -146,3 +147,34 @@ def test_snapshots_from_context(gpu_lib, tmp_path):
         assert (tmp_path / "bins.dat").read_text() == (tmp_path / "bins_ref.dat").read_text()
         sim.particles_snapshot(0, tmp_path / "e.dat")
         np.testing.assert_array_equal(cg.read_particles_file(tmp_path / "e.dat"), sim.particles(0))
+
+
+def test_reference_shaped_main_matches_program(first_run, tmp_path):
+    """A main in the shape of main.cu, calling the reference-named functions
+    of libcupic_ref.so from a bin/ directory with ../input and ../output,
+    writes the same particle files as cupic_run."""
+    d, out = first_run
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    build = os.path.join(root, "cupic_gb300", "_build")
+    exe = tmp_path / "ref_shape_main"
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(root, "include"),
+                    os.path.join(root, "tests", "ref_shape_main.cpp"), "-o", str(exe), "-L", build,
+                    "-lcupic_ref", "-lcupic_gpu", f"-Wl,-rpath,{build}"], check=True)
+    w = tmp_path / "case"
+    for sub in ("bin", "input", "output/particles"):
+        (w / sub).mkdir(parents=True)
+    (w / "input" / "input_data").write_text(INPUT)
+    r = subprocess.run([str(exe)], cwd=w / "bin", capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    lines = r.stdout.splitlines()
+    assert lines[0] == out[0] and [l for l in lines if l.startswith("t = ")] == \
+        [l for l in out if l.startswith("t = ")]
+    for i in (0, 10, 20):
+        for s in ("electrons", "ions"):
+            a = (d / "output" / "particles" / f"{s}_t_{i}.dat").read_text()
+            b = (w / "output" / "particles" / f"{s}_t_{i}.dat").read_text()
+            assert a == b, f"{s} t={i}"
+    for i in (10, 20):
+        for f in (f"charge_t_{i - 1}.dat", f"potential_t_{i - 1}.dat", f"bm_electrons_t_{i}.dat",
+                  f"bins_electrons_t_{i}.dat"):
+            assert (w / "output" / f).stat().st_size > 0, f
