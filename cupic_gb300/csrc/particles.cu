@@ -30,23 +30,25 @@ __device__ __forceinline__ void raise_flags(Ctl *ctl, uint32_t f) {
 
 // Charge deposition into shared memory by cell moments.  For the particles
 // of a cell, with 16-bit fixed-point offsets FX, FY in [0, 65536] and
-// GX = 65536-FX, GY = 65536-FY, the four node sums of q*weight follow exactly
-// from four integer moments of the cell:
-//   sum q GX GY = 65536^2 M1 - 65536 (MX + MY) + MXY      (lower-left node)
-//   sum q FX GY = 65536 MX - MXY                          (lower-right)
-//   sum q GX FY = 65536 MY - MXY                          (upper-left)
-//   sum q FX FY = MXY                                     (upper-right)
-// with M1 = sum q, MX = sum q FX, MY = sum q FY, MXY = sum q FX FY.  Shared
-// memory atomics are native for 32-bit integers only, so a particle adds q,
-// q FX, q FY and the two 16-bit halves of q FX FY to five int32 moment
-// planes; within kFoldParticles particles none of them can overflow, and
-// fold() turns the moments into int64 node sums that often.  flush() adds
-// the node sums to global memory once.  Deposits whose cell row is outside
-// the tile go straight to global memory as int64 node weights.
-constexpr int kFoldParticles = 16384;
+// GX = 65536-FX, GY = 65536-FY, the four node sums of the weights follow
+// exactly from four integer moments of the cell:
+//   sum GX GY = 65536^2 M1 - 65536 (MX + MY) + MXY      (lower-left node)
+//   sum FX GY = 65536 MX - MXY                          (lower-right)
+//   sum GX FY = 65536 MY - MXY                          (upper-left)
+//   sum FX FY = MXY                                     (upper-right)
+// with M1 = count, MX = sum FX, MY = sum FY, MXY = sum FX FY.  Shared memory
+// atomics are native for 32-bit integers only, so a particle adds 1, FX, FY
+// and the two 16-bit halves of FX FY to the five unsigned moments of its
+// cell (stored together, one address per particle).  The moments of one
+// species over at most kFoldParticles particles stay below 2^32; fold(q)
+// turns them into int64 node sums times the species charge q that often and
+// at every change of species.  flush() adds the node sums to global memory
+// once.  Deposits whose cell row is outside the tile go straight to global
+// memory as int64 node weights.
+constexpr int kFoldParticles = 63 * 1024;  // 64512 * 65536 < 2^32
 
 struct RhoMoments {
-  int *m;          // [5][ncr*ncx]: M1, MX, MY, MXY>>16 part, MXY low 16 bits
+  unsigned *m;     // [ncr*ncx][5]: M1, MX, MY, MXY >> 16, MXY & 0xffff
   long long *node; // [(ncr+1)*nnx] node sums of this block
   int crow0, ncr, ncx, nnx;
   unsigned long long *g;
@@ -55,13 +57,13 @@ struct RhoMoments {
     const CicFixed c = cic_fixed(a, x, y);
     const int tr = c.jc - crow0;
     if (tr >= 0 && tr < ncr) {
-      const int k = tr * ncx + c.ic, pl = ncr * ncx;
+      unsigned *mc = m + 5 * (tr * ncx + c.ic);
       const unsigned long long fxy = (unsigned long long)c.FX * (unsigned long long)c.FY;
-      atomicAdd(&m[k], q);
-      atomicAdd(&m[pl + k], q * c.FX);
-      atomicAdd(&m[2 * pl + k], q * c.FY);
-      atomicAdd(&m[3 * pl + k], q * (int)(fxy >> 16));
-      atomicAdd(&m[4 * pl + k], q * (int)(fxy & 0xffffull));
+      atomicAdd(mc, 1u);
+      atomicAdd(mc + 1, (unsigned)c.FX);
+      atomicAdd(mc + 2, (unsigned)c.FY);
+      atomicAdd(mc + 3, (unsigned)(fxy >> 16));
+      atomicAdd(mc + 4, (unsigned)(fxy & 0xffffull));
     } else {
       const size_t n00 = (size_t)c.jc * nnx + c.ic;
       atomicAdd(&g[n00], (unsigned long long)(q * c.w00));
@@ -71,43 +73,43 @@ struct RhoMoments {
     }
   }
   __device__ __forceinline__ void zero() const {
-    for (int k = threadIdx.x; k < 5 * ncr * ncx; k += blockDim.x) m[k] = 0;
+    for (int k = threadIdx.x; k < 5 * ncr * ncx; k += blockDim.x) m[k] = 0u;
     for (int k = threadIdx.x; k < (ncr + 1) * nnx; k += blockDim.x) node[k] = 0;
   }
-  // moments -> node sums, then clear the moments; callers __syncthreads()
-  // before, and before the next deposit
-  __device__ __forceinline__ void fold() const {
-    const int pl = ncr * ncx;
+  __device__ __forceinline__ long long mxy(int c) const {
+    return (long long)m[5 * c + 3] * 65536 + (long long)m[5 * c + 4];
+  }
+  // moments (of charge q particles) -> node sums, then clear the moments;
+  // callers __syncthreads() before, and before the next deposit
+  __device__ __forceinline__ void fold(int q) const {
     for (int k = threadIdx.x; k < (ncr + 1) * nnx; k += blockDim.x) {
       const int j = k / nnx, i = k - j * nnx;
       long long v = 0;
       if (i < ncx && j < ncr) {  // this node is the lower-left corner of cell (i, j)
         const int c = j * ncx + i;
-        const long long mxy = (long long)m[3 * pl + c] * 65536 + m[4 * pl + c];
-        v += (long long)m[c] * 4294967296ll - 65536ll * ((long long)m[pl + c] + m[2 * pl + c]) + mxy;
+        v += (long long)m[5 * c] * 4294967296ll -
+             65536ll * ((long long)m[5 * c + 1] + (long long)m[5 * c + 2]) + mxy(c);
       }
       if (i >= 1 && j < ncr) {  // lower-right corner of cell (i-1, j)
         const int c = j * ncx + i - 1;
-        const long long mxy = (long long)m[3 * pl + c] * 65536 + m[4 * pl + c];
-        v += 65536ll * m[pl + c] - mxy;
+        v += 65536ll * (long long)m[5 * c + 1] - mxy(c);
       }
       if (i < ncx && j >= 1) {  // upper-left corner of cell (i, j-1)
         const int c = (j - 1) * ncx + i;
-        const long long mxy = (long long)m[3 * pl + c] * 65536 + m[4 * pl + c];
-        v += 65536ll * m[2 * pl + c] - mxy;
+        v += 65536ll * (long long)m[5 * c + 2] - mxy(c);
       }
       if (i >= 1 && j >= 1) {  // upper-right corner of cell (i-1, j-1)
-        const int c = (j - 1) * ncx + i - 1;
-        v += (long long)m[3 * pl + c] * 65536 + m[4 * pl + c];
+        v += mxy((j - 1) * ncx + i - 1);
       }
-      node[k] += v;
+      node[k] += q * v;
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < 5 * pl; k += blockDim.x) m[k] = 0;
+    for (int k = threadIdx.x; k < 5 * ncr * ncx; k += blockDim.x) m[k] = 0u;
   }
-  // fold + add the node sums to global memory; callers __syncthreads() before
-  __device__ __forceinline__ void flush(int nny) {
-    fold();
+  // fold (charge q) + add the node sums to global memory; callers
+  // __syncthreads() before
+  __device__ __forceinline__ void flush(int nny, int q) {
+    fold(q);
     __syncthreads();
     for (int k = threadIdx.x; k < (ncr + 1) * nnx; k += blockDim.x) {
       const long long v = node[k];
@@ -173,15 +175,16 @@ __global__ void k_init_particles(SimArgs a) {
 __global__ void k_deposit(SimArgs a) {
   extern __shared__ long long dtile[];
   const int s = blockIdx.x, nnx = a.nnx, ncx = a.ncx;
-  RhoMoments T{reinterpret_cast<int *>(dtile + 2 * nnx), dtile, s, 1, ncx, nnx, a.rho[a.ctl->cur]};
+  RhoMoments T{reinterpret_cast<unsigned *>(dtile + 2 * nnx), dtile, s, 1, ncx, nnx,
+               a.rho[a.ctl->cur]};
   T.zero();
   __syncthreads();
-  int since = 0;
   for (int sp = 0; sp < 2; ++sp) {
     const SpeciesDev &S = a.sp[sp];
     const float4 *row = S.parts + S.seg[s];
     const int n = S.cnt[s];
     const int q = sp == 0 ? -1 : 1;
+    int since = 0;
     for (int base = 0; base < n; base += blockDim.x) {
       const int k = base + threadIdx.x;
       if (k < n) {
@@ -189,16 +192,21 @@ __global__ void k_deposit(SimArgs a) {
         T.deposit(a, p.x, p.y, q);
       }
       since += blockDim.x;
-      if (since >= kFoldParticles) {  // block-uniform
+      if (since + (int)blockDim.x > kFoldParticles) {  // block-uniform
         __syncthreads();
-        T.fold();
+        T.fold(q);
         __syncthreads();
         since = 0;
       }
     }
+    __syncthreads();
+    if (sp == 0) {
+      T.fold(q);  // a species' moments are folded before the next one's
+      __syncthreads();
+    } else {
+      T.flush(a.nny, q);
+    }
   }
-  __syncthreads();
-  T.flush(a.nny);
 }
 
 // zero the accumulator the next deposit writes (rho[cur^1])
@@ -250,7 +258,7 @@ __global__ void k_leapfrog_start(SimArgs a) {
 namespace {
 constexpr int kPB = 512;       // threads
 constexpr int kPPT = 2;        // particles per thread per chunk
-constexpr int kStages = 3;     // chunks in flight
+constexpr int kStages = 2;     // chunks in flight
 constexpr int kCH = kPB * kPPT;
 // scan entries per chunk: one per (particle slot j, warp), 32 particles each
 constexpr int kNE = kPPT * (kPB / 32);
@@ -281,7 +289,7 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
   float4 *stage = reinterpret_cast<float4 *>(push_raw);
   float4 *etile = stage + kStages * kCH;                          // 2*ncx node pairs
   long long *tnode = reinterpret_cast<long long *>(etile + 2 * ncx);  // node rows s-1..s+2
-  int *tmom = reinterpret_cast<int *>(tnode + 4 * nnx);               // cell rows s-1..s+1
+  unsigned *tmom = reinterpret_cast<unsigned *>(tnode + 4 * nnx);     // cell rows s-1..s+1
   __shared__ __align__(8) uint64_t full[kStages];
   __shared__ uint32_t wsum[2][NE];  // per-entry packed counts, alternate chunks
   __shared__ unsigned long long s_cnt[4];
@@ -309,6 +317,7 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
     }
   }
   RhoMoments T{tmom, tnode, s - 1, 3, ncx, nnx, a.rho[ctl->cur ^ 1]};
+  int since_fold = 0;  // chunks deposited since the last fold
   T.zero();
   for (int k = tid; k < 2 * ncx; k += kPB) {
     const int r = k / ncx, i = k - r * ncx;
@@ -421,9 +430,13 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
       S.nup[s] = min(c_up, S.stage_cap);
       S.ndown[s] = min(c_dn, S.stage_cap);
     }
-    if ((k + 1) % (kFoldParticles / kCH) == 0 && k + 1 < nct) {  // block-uniform
+    // fold at the end of a species and before the moments could overflow
+    // (block-uniform); the next deposits follow the next chunk's barrier
+    ++since_fold;
+    if (k + 1 < nct && (k + 1 == nc0 || (since_fold + 1) * kCH > kFoldParticles)) {
       __syncthreads();
-      T.fold();  // the next deposits follow the next chunk's barriers
+      T.fold(qc);
+      since_fold = 0;
     }
   }
   for (int sp = 0; sp < 2; ++sp) {  // rows with no particles of a species
@@ -446,7 +459,7 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
     if (s_cnt[2 * tid]) atomicAdd(&ctl->absorbed[tid], s_cnt[2 * tid]);
     if (s_cnt[2 * tid + 1]) atomicAdd(&ctl->removed[tid], s_cnt[2 * tid + 1]);
   }
-  T.flush(a.nny);
+  T.flush(a.nny, nct > nc0 ? 1 : -1);  // the moments hold the last species' particles
   fl = __reduce_or_sync(kFull, fl);
   if (lane == 0) raise_flags(ctl, fl);
 }
