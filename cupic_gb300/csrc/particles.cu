@@ -41,16 +41,15 @@ __device__ __forceinline__ void raise_flags(Ctl *ctl, uint32_t f) {
 // and the two 16-bit halves of FX FY to the five unsigned moments of its
 // cell (stored together, one address per particle).  The moments of one
 // species over at most kFoldParticles particles stay below 2^32; fold(q)
-// turns them into int64 node sums times the species charge q that often and
-// at every change of species.  flush() adds the node sums to global memory
-// once.  Deposits whose cell row is outside the tile go straight to global
-// memory as int64 node weights.
+// turns them into int64 node sums times the species charge q, added to
+// global memory, that often and at every change of species.  Deposits whose
+// cell row is outside the tile go straight to global memory as int64 node
+// weights.
 constexpr int kFoldParticles = 63 * 1024;  // 64512 * 65536 < 2^32
 
 struct RhoMoments {
   unsigned *m;     // [ncr*ncx][5]: M1, MX, MY, MXY >> 16, MXY & 0xffff
-  long long *node; // [(ncr+1)*nnx] node sums of this block
-  int crow0, ncr, ncx, nnx;
+  int crow0, ncr, ncx, nnx, nny;
   unsigned long long *g;
 
   __device__ __forceinline__ void deposit(const SimArgs &a, float x, float y, int q) const {
@@ -74,13 +73,13 @@ struct RhoMoments {
   }
   __device__ __forceinline__ void zero() const {
     for (int k = threadIdx.x; k < 5 * ncr * ncx; k += blockDim.x) m[k] = 0u;
-    for (int k = threadIdx.x; k < (ncr + 1) * nnx; k += blockDim.x) node[k] = 0;
   }
   __device__ __forceinline__ long long mxy(int c) const {
     return (long long)m[5 * c + 3] * 65536 + (long long)m[5 * c + 4];
   }
-  // moments (of charge q particles) -> node sums, then clear the moments;
-  // callers __syncthreads() before, and before the next deposit
+  // moments (of charge q particles) -> node sums added to global memory,
+  // then clear the moments; callers __syncthreads() before, and before the
+  // next deposit
   __device__ __forceinline__ void fold(int q) const {
     for (int k = threadIdx.x; k < (ncr + 1) * nnx; k += blockDim.x) {
       const int j = k / nnx, i = k - j * nnx;
@@ -101,27 +100,17 @@ struct RhoMoments {
       if (i >= 1 && j >= 1) {  // upper-right corner of cell (i-1, j-1)
         v += mxy((j - 1) * ncx + i - 1);
       }
-      node[k] += q * v;
+      const int r = crow0 + j;
+      if (v != 0 && r >= 0 && r < nny)
+        atomicAdd(&g[(size_t)r * nnx + i], (unsigned long long)(q * v));
     }
     __syncthreads();
     for (int k = threadIdx.x; k < 5 * ncr * ncx; k += blockDim.x) m[k] = 0u;
   }
-  // fold (charge q) + add the node sums to global memory; callers
-  // __syncthreads() before
-  __device__ __forceinline__ void flush(int nny, int q) {
-    fold(q);
-    __syncthreads();
-    for (int k = threadIdx.x; k < (ncr + 1) * nnx; k += blockDim.x) {
-      const long long v = node[k];
-      const int r = crow0 + k / nnx;
-      if (v != 0 && r >= 0 && r < nny)
-        atomicAdd(&g[(size_t)r * nnx + (k % nnx)], (unsigned long long)v);
-    }
-  }
 };
 
 __host__ __device__ constexpr size_t rho_moment_bytes(int ncr, int ncx) {
-  return (size_t)5 * ncr * ncx * sizeof(int) + (size_t)(ncr + 1) * (ncx + 1) * sizeof(long long);
+  return (size_t)5 * ncr * ncx * sizeof(unsigned);
 }
 
 // classification of a pushed particle listed in row s (s < 0: injected)
@@ -173,10 +162,9 @@ __global__ void k_init_particles(SimArgs a) {
 // (mesh.cu:162-293; int64 fixed point, so the sum is order independent)
 // ---------------------------------------------------------------------------
 __global__ void k_deposit(SimArgs a) {
-  extern __shared__ long long dtile[];
+  extern __shared__ unsigned dtile[];
   const int s = blockIdx.x, nnx = a.nnx, ncx = a.ncx;
-  RhoMoments T{reinterpret_cast<unsigned *>(dtile + 2 * nnx), dtile, s, 1, ncx, nnx,
-               a.rho[a.ctl->cur]};
+  RhoMoments T{dtile, s, 1, ncx, nnx, a.nny, a.rho[a.ctl->cur]};
   T.zero();
   __syncthreads();
   for (int sp = 0; sp < 2; ++sp) {
@@ -200,12 +188,8 @@ __global__ void k_deposit(SimArgs a) {
       }
     }
     __syncthreads();
-    if (sp == 0) {
-      T.fold(q);  // a species' moments are folded before the next one's
-      __syncthreads();
-    } else {
-      T.flush(a.nny, q);
-    }
+    T.fold(q);  // a species' moments are folded before the next one's
+    __syncthreads();
   }
 }
 
@@ -276,10 +260,10 @@ __device__ __forceinline__ uint32_t field2(uint32_t v) { return v >> 21; }
 
 size_t push_smem_bytes(int nnx) {
   return (size_t)kStages * kCH * sizeof(float4) + rho_moment_bytes(3, nnx - 1) +
-         (size_t)2 * (nnx - 1) * sizeof(float4);
+         (size_t)2 * nnx * sizeof(float2);
 }
 
-__global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
+__global__ void __launch_bounds__(kPB, 3) k_push_deposit(SimArgs a) {
   extern __shared__ __align__(128) unsigned char push_raw[];
   constexpr int NW = kPB / 32;
   constexpr int NE = kNE;  // scan entries per chunk, (j, warp) in j-major order
@@ -287,9 +271,8 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
   const int nnx = a.nnx;
   const int ncx = a.ncx;
   float4 *stage = reinterpret_cast<float4 *>(push_raw);
-  float4 *etile = stage + kStages * kCH;                          // 2*ncx node pairs
-  long long *tnode = reinterpret_cast<long long *>(etile + 2 * ncx);  // node rows s-1..s+2
-  unsigned *tmom = reinterpret_cast<unsigned *>(tnode + 4 * nnx);     // cell rows s-1..s+1
+  float2 *etile = reinterpret_cast<float2 *>(stage + kStages * kCH);  // node rows s, s+1
+  unsigned *tmom = reinterpret_cast<unsigned *>(etile + 2 * nnx);      // cell rows s-1..s+1
   __shared__ __align__(8) uint64_t full[kStages];
   __shared__ uint32_t wsum[2][NE];  // per-entry packed counts, alternate chunks
   __shared__ unsigned long long s_cnt[4];
@@ -316,14 +299,10 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
       bulk_g2s(stage + k * kCH, (sp1 ? row1 : row0) + (size_t)q * kCH, (uint32_t)cnt * 16u, &full[k]);
     }
   }
-  RhoMoments T{tmom, tnode, s - 1, 3, ncx, nnx, a.rho[ctl->cur ^ 1]};
+  RhoMoments T{tmom, s - 1, 3, ncx, nnx, a.nny, a.rho[ctl->cur ^ 1]};
   int since_fold = 0;  // chunks deposited since the last fold
   T.zero();
-  for (int k = tid; k < 2 * ncx; k += kPB) {
-    const int r = k / ncx, i = k - r * ncx;
-    const float2 e0 = a.E[(size_t)(s + r) * nnx + i], e1 = a.E[(size_t)(s + r) * nnx + i + 1];
-    etile[k] = make_float4(e0.x, e0.y, e1.x, e1.y);
-  }
+  for (int k = tid; k < 2 * nnx; k += kPB) etile[k] = a.E[(size_t)s * nnx + k];
   __syncthreads();
 
   uint32_t fl = 0;
@@ -352,7 +331,7 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
       if (idx < cnt) {
         float4 v = stage[st * kCH + idx];
         float ex, ey;
-        gather_tile4(a, etile, v.x, v.y, s, ex, ey);
+        gather_tile(a, etile, v.x, v.y, s, ex, ey);
         v.z = __fmaf_rn(dtqm, ex, v.z);
         v.w = __fmaf_rn(dtqm, ey, v.w);
         v.x = __fmaf_rn(a.dt, v.z, v.x);
@@ -459,7 +438,7 @@ __global__ void __launch_bounds__(kPB) k_push_deposit(SimArgs a) {
     if (s_cnt[2 * tid]) atomicAdd(&ctl->absorbed[tid], s_cnt[2 * tid]);
     if (s_cnt[2 * tid + 1]) atomicAdd(&ctl->removed[tid], s_cnt[2 * tid + 1]);
   }
-  T.flush(a.nny, nct > nc0 ? 1 : -1);  // the moments hold the last species' particles
+  T.fold(nct > nc0 ? 1 : -1);  // the moments hold the last species' particles
   fl = __reduce_or_sync(kFull, fl);
   if (lane == 0) raise_flags(ctl, fl);
 }
