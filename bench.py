@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["cupic", "reference"], default="cupic")
-    ap.add_argument("--workload", choices=["large", "small", "tiny"], default="large")
+    ap.add_argument("--workload", choices=["large", "precision", "small", "tiny"], default="large")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncy", type=int, default=0,
@@ -103,7 +103,9 @@ def workload_desc(p):
     ppc = p.ppr // p.ncx
     return (f"{p.ncx}x{p.ncy} cells, ds={p.ds}, {ppc} particles per cell per species, "
             f"mi/me={p.mi:g}, Ti/Te={p.kti:g}, phi_p={p.phi_p:g}, dt={p.dt:g}, "
-            f"Jacobi {p.min_sweeps}-{p.max_sweeps} sweeps, seed {p.seed}")
+            f"Jacobi {p.min_sweeps}-{p.max_sweeps} sweeps" +
+            (f" to an FP64 residual of {p.tol:g} (correction every {p.refine_every})"
+             if p.refine_every else "") + f", seed {p.seed}")
 
 
 def measured_peaks():
@@ -377,7 +379,9 @@ def run_cupic(args, world, rank, local):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": tmax * 1e3 / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if not p.refine_every else
+                     f"f32 sweeps, f64 residual and correction every {p.refine_every} sweeps",
             "data": "synthetic: seeded uniform positions, Maxwellian velocities (Philox4x32-10)",
             "config": {"workload": workload_desc(p), "ncx": p.ncx, "ncy": p.ncy,
                        "particles_per_step": mean_particles, "nodes": nodes,

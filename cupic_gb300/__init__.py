@@ -350,6 +350,13 @@ class Sim:
         _ok(self.L.cupic_get_phi_f32(self.h, _ptr(o, ctypes.c_float)), "get_phi")
         return o.reshape(self.p.nny, self.p.nnx)
 
+    def phi64(self):
+        """The potential as doubles: the FP64 potential of the precision form
+        (refine_every > 0), else the FP32 one widened."""
+        o = np.empty(self.nnodes)
+        _ok(self.L.cupic_get_phi(self.h, _ptr(o, ctypes.c_double)), "get_phi")
+        return o.reshape(self.p.nny, self.p.nnx)
+
     def set_phi(self, phi):
         a = np.ascontiguousarray(phi, dtype=np.float64).ravel()
         _ok(self.L.cupic_set_phi(self.h, _ptr(a, ctypes.c_double)), "set_phi")

@@ -39,6 +39,12 @@ struct cupic_ctx {
   unsigned *jflags = nullptr;  // [G+1]: per-CTA sweep counters, then the barrier
   float *jres = nullptr;
   float *jhalo = nullptr;
+  // precision form of the solve (refine_every > 0): FP64 potential, FP32
+  // residual source and correction, the residual's max norm
+  double *phi64 = nullptr;
+  float *rr = nullptr, *dl = nullptr;
+  unsigned long long *maxr = nullptr;
+  void *h_pin = nullptr;  // pinned: [0] max-norm bits, [1] {sweeps, residual}
   // graph of one step
   cudaGraphExec_t graph = nullptr;
   bool graph_ok = false;
@@ -398,13 +404,68 @@ JacobiArgs jargs(const cupic_ctx *c, double tol, int mn, int mx, int chk, int fi
   return J;
 }
 
+int set_phi_both(cupic_ctx *c, const double *phi) {
+  const size_t n = (size_t)c->a.nnx * c->a.nny;
+  std::vector<float> h(n);
+  for (size_t k = 0; k < n; ++k) h[k] = (float)phi[k];
+  CU(cudaMemcpy(c->a.phi, h.data(), n * sizeof(float), cudaMemcpyHostToDevice));
+  if (c->phi64) CU(cudaMemcpy(c->phi64, phi, n * sizeof(double), cudaMemcpyHostToDevice));
+  return CUPIC_OK;
+}
+
 int set_linear_phi(cupic_ctx *c) {
   const int nnx = c->a.nnx, nny = c->a.nny;
-  std::vector<float> h((size_t)nnx * nny);
+  std::vector<double> h((size_t)nnx * nny);
   for (int j = 0; j < nny; ++j)
     for (int i = 0; i < nnx; ++i)  // init.cu:235-241
-      h[(size_t)j * nnx + i] = (float)((1.0 - (double)j / (double)c->p.ncy) * c->p.phi_p);
-  CU(cudaMemcpy(c->a.phi, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
+      h[(size_t)j * nnx + i] = (1.0 - (double)j / (double)c->p.ncy) * c->p.phi_p;
+  return set_phi_both(c, h.data());
+}
+
+// Precision form (refine_every = m > 0): every m FP32 Jacobi sweeps on the
+// correction, an FP64 residual and update; stops when the residual's max
+// norm is below tol after at least mn sweeps, or at mx sweeps.  The host
+// reads the norm once per m sweeps.
+int refine_solve(cupic_ctx *c, double tol, int mn, int mx, int field, int write_stats) {
+  const int m = c->p.refine_every;
+  unsigned long long *hbits = static_cast<unsigned long long *>(c->h_pin);
+  int sweeps = 0;
+  double res = 0.0;
+  for (;;) {
+    CU(launch_r64_residual(c->a, c->phi64, c->rr, c->dl, c->maxr, c->stream));
+    CU(cudaMemcpyAsync(hbits, c->maxr, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                       c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    memcpy(&res, hbits, sizeof(double));
+    if ((sweeps >= mn && res < tol) || sweeps >= mx) break;
+    const int k = std::min(m, mx - sweeps);
+    JacobiArgs J = jargs(c, 0.0, k, k, k, 0);
+    J.write_stats = 0;
+    J.phi = c->dl;
+    J.src = c->rr;
+    CU(launch_jacobi(c->a, J, c->stream));
+    CU(launch_r64_update(c->a, c->phi64, c->dl, c->stream));
+    sweeps += k;
+  }
+  if (field) CU(launch_r64_field(c->a, c->phi64, c->stream));
+  if (write_stats) {
+    struct {
+      int32_t sweeps;
+      float residual;
+    } st = {sweeps, (float)res};
+    static_assert(offsetof(Ctl, residual) == offsetof(Ctl, sweeps) + 4, "Ctl layout");
+    memcpy(hbits + 1, &st, sizeof(st));
+    CU(cudaMemcpyAsync(&c->ctl->sweeps, hbits + 1, sizeof(st), cudaMemcpyHostToDevice, c->stream));
+  }
+  return CUPIC_OK;
+}
+
+// the solve of a step or stage call, FP32 or in the precision form
+int run_solve(cupic_ctx *c, double tol, int mn, int mx, int chk, int field, int write_stats = 1) {
+  if (c->p.refine_every > 0) return refine_solve(c, tol, mn, mx, field, write_stats);
+  JacobiArgs J = jargs(c, tol, mn, mx, chk, field);
+  J.write_stats = write_stats;
+  CU(launch_jacobi(c->a, J, c->stream));
   return CUPIC_OK;
 }
 
@@ -450,9 +511,7 @@ int finish(cupic_ctx *c) {
 // One step: solve + field, then the injection draws on the side stream while
 // the main stream clears the next charge, pushes and appends the movers;
 // the injected particles are appended once both branches are done.
-int enqueue_step(cupic_ctx *c) {
-  const cupic_params &p = c->p;
-  CU(launch_jacobi(c->a, jargs(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1), c->stream));
+int enqueue_after_solve(cupic_ctx *c) {
   CU(cudaEventRecord(c->ev_fork, c->stream));
   CU(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
   CU(launch_inject_draw(c->a, c->side));
@@ -464,6 +523,13 @@ int enqueue_step(cupic_ctx *c) {
   CU(launch_inject_append(c->a, c->stream));
   CU(launch_finalize(c->a, c->stream));
   return CUPIC_OK;
+}
+
+int enqueue_step(cupic_ctx *c) {
+  const cupic_params &p = c->p;
+  int rc = run_solve(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1);
+  if (rc) return rc;
+  return enqueue_after_solve(c);
 }
 
 int capture_step(cupic_ctx *c) {
@@ -690,6 +756,12 @@ int cupic_create(const cupic_params *pin, int device, cupic_ctx **out) {
       dalloc(&a.rho[1], nodes) || dalloc(&c->ctl, 1))
     return fail(CUPIC_ERR_NOMEM);
   a.ctl = c->ctl;
+  if (c->p.refine_every > 0) {
+    if (dalloc(&c->phi64, nodes) || dalloc(&c->rr, nodes) || dalloc(&c->dl, nodes) ||
+        dalloc(&c->maxr, 1) || cudaMallocHost(&c->h_pin, 64) != cudaSuccess)
+      return fail(CUPIC_ERR_NOMEM);
+    if (cudaMemset(c->phi64, 0, nodes * sizeof(double))) return fail(CUPIC_ERR_CUDA);
+  }
   if (cudaMemset(a.phi, 0, nodes * sizeof(float)) || cudaMemset(a.E, 0, nodes * sizeof(float2)) ||
       cudaMemset(a.rho[0], 0, nodes * 8) || cudaMemset(a.rho[1], 0, nodes * 8) ||
       cudaMemset(c->ctl, 0, sizeof(Ctl)))
@@ -724,6 +796,11 @@ int cupic_destroy(cupic_ctx *c) {
   cudaFree(c->jflags);
   cudaFree(c->jres);
   cudaFree(c->jhalo);
+  cudaFree(c->phi64);
+  cudaFree(c->rr);
+  cudaFree(c->dl);
+  cudaFree(c->maxr);
+  if (c->h_pin) cudaFreeHost(c->h_pin);
   if (c->side) cudaStreamSynchronize(c->side);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->ev_join) cudaEventDestroy(c->ev_join);
@@ -777,8 +854,8 @@ int cupic_init_plasma(cupic_ctx *c) {
   rc = deposit_current(c);
   if (rc) return rc;
   const cupic_params &p = c->p;
-  CU(launch_jacobi(c->a, jargs(c, p.init_tol, p.init_min_sweeps, p.init_max_sweeps, p.check_every, 1),
-                   c->stream));
+  rc = run_solve(c, p.init_tol, p.init_min_sweeps, p.init_max_sweeps, p.check_every, 1);
+  if (rc) return rc;
   CU(launch_leapfrog_start(c->a, c->stream));
   rc = sync_check(c);
   if (rc) return rc;
@@ -797,8 +874,8 @@ int cupic_init_mesh(cupic_ctx *c) {
   rc = deposit_current(c);
   if (rc) return rc;
   const cupic_params &p = c->p;
-  CU(launch_jacobi(c->a, jargs(c, p.init_tol, p.init_min_sweeps, p.init_max_sweeps, p.check_every, 1),
-                   c->stream));
+  rc = run_solve(c, p.init_tol, p.init_min_sweeps, p.init_max_sweeps, p.check_every, 1);
+  if (rc) return rc;
   rc = sync_check(c);
   if (rc) return rc;
   rc = cupic_set_time(c, (int64_t)p.n_ini + 1, p.n_ini * p.dt + p.dt, -1.0, -1.0);
@@ -902,16 +979,21 @@ int cupic_poisson_solver(cupic_ctx *c, double max_error, int32_t mn, int32_t mx,
     chk = c->p.check_every;
   }
   if (mx < 0) return CUPIC_ERR_ARG;
-  CU(launch_jacobi(c->a, jargs(c, max_error, mn, mx, chk, 0), c->stream));
+  int rc = run_solve(c, max_error, mn, mx, chk, 0);
+  if (rc) return rc;
   return finish(c);
 }
 
 int cupic_field_solver(cupic_ctx *c) {
   if (!c) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
-  JacobiArgs J = jargs(c, 0.0, 0, 0, 1, 1);
-  J.write_stats = 0;
-  CU(launch_jacobi(c->a, J, c->stream));
+  if (c->p.refine_every > 0) {
+    CU(launch_r64_field(c->a, c->phi64, c->stream));
+  } else {
+    JacobiArgs J = jargs(c, 0.0, 0, 0, 1, 1);
+    J.write_stats = 0;
+    CU(launch_jacobi(c->a, J, c->stream));
+  }
   return finish(c);
 }
 
@@ -946,6 +1028,14 @@ int cupic_step(cupic_ctx *c, int32_t nsteps) {
   if (!c->rho_valid) {
     int rc = deposit_current(c);
     if (rc) return rc;
+  }
+  if (c->p.refine_every > 0) {  // the solve reads its residual norm on the host: no graph
+    for (int i = 0; i < nsteps; ++i) {
+      int rc = enqueue_step(c);
+      if (rc) return rc;
+      c->host_cur ^= 1;
+    }
+    return CUPIC_OK;
   }
   if (!c->graph_ok) {
     int rc = capture_step(c);
@@ -1027,7 +1117,13 @@ int cupic_step_timed(cupic_ctx *c, int32_t nsteps, float *phase_ms, int32_t npha
     // main-stream kernel; the inject phase is the wait for the side branch
     // (draws) plus the append
     cudaEvent_t *q = &ev[(size_t)s * per + 1];
-    e = launch_jacobi(c->a, J, c->stream);
+    if (c->p.refine_every > 0) {
+      const int r = refine_solve(c, p.tol, p.min_sweeps, p.max_sweeps, 1, 1);
+      if (r) rc = r;
+      e = r ? cudaErrorUnknown : cudaSuccess;
+    } else {
+      e = launch_jacobi(c->a, J, c->stream);
+    }
     if (e == cudaSuccess) e = cudaEventRecord(q[0], c->stream);
     if (e == cudaSuccess) e = cudaEventRecord(c->ev_fork, c->stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
@@ -1123,6 +1219,12 @@ int cupic_get_phi_f32(cupic_ctx *c, float *phi) {
 
 int cupic_get_phi(cupic_ctx *c, double *phi) {
   if (!c || !phi) return CUPIC_ERR_ARG;
+  if (c->phi64) {  // the precision form's FP64 potential
+    CU(cudaSetDevice(c->device));
+    CU(cudaStreamSynchronize(c->stream));
+    CU(cudaMemcpy(phi, c->phi64, sizeof(double) * c->a.nnx * c->a.nny, cudaMemcpyDeviceToHost));
+    return CUPIC_OK;
+  }
   std::vector<float> h((size_t)c->a.nnx * c->a.nny);
   int rc = cupic_get_phi_f32(c, h.data());
   if (rc) return rc;
@@ -1133,11 +1235,8 @@ int cupic_get_phi(cupic_ctx *c, double *phi) {
 int cupic_set_phi(cupic_ctx *c, const double *phi) {
   if (!c || !phi) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
-  std::vector<float> h((size_t)c->a.nnx * c->a.nny);
-  for (size_t k = 0; k < h.size(); ++k) h[k] = (float)phi[k];
   CU(cudaStreamSynchronize(c->stream));
-  CU(cudaMemcpy(c->a.phi, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice));
-  return CUPIC_OK;
+  return set_phi_both(c, phi);
 }
 
 int cupic_get_field_f32(cupic_ctx *c, float *ex, float *ey) {

@@ -93,6 +93,8 @@ struct JacobiArgs {
   unsigned int *bar;      // [1] grid barrier counter
   float *res_cta;         // [2*G] per-CTA max |dphi| of a checked sweep
   float *halo;            // [2 parity][G][2 sides][depth rows][pitch]
+  float *phi;             // the potential solved for; NULL: a.phi
+  const float *src;       // FP32 source per node; NULL: the charge accumulator a.rho[cur]
 };
 
 // ---------------------------------------------------------------------------

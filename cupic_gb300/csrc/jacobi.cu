@@ -242,18 +242,23 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
   float *const bsrc = jsm + (size_t)2 * cap * P;  // same row indexing as the buffers
   Ctl *ctl = a.ctl;
 
+  float *const phi = J.phi ? J.phi : a.phi;
   const long long *acc = reinterpret_cast<const long long *>(a.rho[ctl->cur]);
   for (int lr = 0; lr < nrows; ++lr) {
     const int j = lo + lr;
     const size_t rb = (size_t)j * nnx;
     const bool interior = j >= 1 && j <= nny - 2;
     for (int i = tid; i < nnx; i += kJBlock) {
-      const float v = a.phi[rb + i];
+      const float v = phi[rb + i];
       buf0[lr * P + i] = v;
       buf1[lr * P + i] = v;
       if (interior) {
-        const long long f = (i == 0 || i == nnx - 1) ? acc[rb] + acc[rb + nnx - 1] : acc[rb + i];
-        bsrc[lr * P + i] = __double2float_rn((double)f * a.cb);
+        if (J.src) {
+          bsrc[lr * P + i] = J.src[rb + i];
+        } else {
+          const long long f = (i == 0 || i == nnx - 1) ? acc[rb] + acc[rb + nnx - 1] : acc[rb + i];
+          bsrc[lr * P + i] = __double2float_rn((double)f * a.cb);
+        }
       }
     }
   }
@@ -425,7 +430,7 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
   // rows r0-1 and r1 are current: either just exchanged or updated in the
   // last sweep of an unfinished temporal block.
   for (int lr = o0; lr < o1; ++lr)
-    for (int i = tid; i < nnx; i += kJBlock) a.phi[(size_t)(lo + lr) * nnx + i] = F[lr * P + i];
+    for (int i = tid; i < nnx; i += kJBlock) phi[(size_t)(lo + lr) * nnx + i] = F[lr * P + i];
   if (J.do_field) {
     for (int lr = o0; lr < o1; ++lr) {
       const float *cr = F + lr * P;

@@ -37,4 +37,10 @@ cudaError_t jacobi_set_smem(size_t bytes);
 cudaError_t jacobi_max_ctas(size_t smem, int *per_sm);
 cudaError_t launch_jacobi(const SimArgs &a, const JacobiArgs &J, cudaStream_t st);
 
+// precision form of the solve (refine.cu)
+cudaError_t launch_r64_residual(const SimArgs &a, const double *phi64, float *rr, float *dl,
+                                unsigned long long *maxr, cudaStream_t st);
+cudaError_t launch_r64_update(const SimArgs &a, double *phi64, const float *dl, cudaStream_t st);
+cudaError_t launch_r64_field(const SimArgs &a, const double *phi64, cudaStream_t st);
+
 }  // namespace cupic

@@ -23,6 +23,7 @@ _PARAM_FIELDS = [
     ("ppr", ctypes.c_int32),
     ("row_slack", ctypes.c_double), ("stage_frac", ctypes.c_double),
     ("seed", ctypes.c_uint64),
+    ("refine_every", ctypes.c_int32),
 ]
 
 
@@ -79,6 +80,9 @@ def workload_params(name="small", **over):
             (n=800), mi/me=1836, Ti/Te=0.1, phi_p=-5, dt=0.05, 200 fixed
             Jacobi sweeps, seed 1.
     tiny  : 16x32 cells, 8 particles per cell, for quick tests.
+    precision : the large workload with the precision form of the solve:
+            FP32 sweeps, an FP64 residual and correction every 32 sweeps,
+            to a max-norm residual of 1e-10 (at most 2000 sweeps a step).
     """
     p = Params()
     p.ds, p.dt = 0.5, 0.05
@@ -102,6 +106,12 @@ def workload_params(name="small", **over):
         p.init_tol, p.init_min_sweeps, p.init_max_sweeps = 0.0, 200, 200
         p.check_every = 200  # fixed sweep count: only the last sweep's residual is reported
         p.seed = 1
+    elif name == "precision":
+        p = workload_params("large")
+        p.refine_every = 32
+        p.tol, p.min_sweeps, p.max_sweeps = 1e-10, 32, 2000
+        p.init_tol, p.init_min_sweeps, p.init_max_sweeps = 1e-10, 32, 20000
+        p.check_every = 32
     elif name == "tiny":
         p.ncx, p.ncy = 16, 32
         p.n = 64.0

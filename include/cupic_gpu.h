@@ -96,6 +96,14 @@ typedef struct cupic_params {
   /* seed of the counter-based generator (Philox4x32-10) used for the
    * initial plasma and the injected flux */
   uint64_t seed;
+  /* Precision form of the Poisson solve.  0: FP32 Jacobi with the stop rule
+   * above.  m > 0: the potential is kept in FP64; every m FP32 Jacobi sweeps
+   * solve for a correction from the FP64 residual b - A phi of the
+   * 5-point operator, which is added in FP64.  The solve stops when that
+   * residual's max norm (in the units of b = ds^2 rho / eps0) is below tol
+   * (init_tol for the initial solve) after at least min_sweeps sweeps, or
+   * at max_sweeps; the field is derived in FP64. */
+  int32_t refine_every;
 } cupic_params;
 
 /* Per-step counters (absorbed = crossed y<0 into the probe; removed =

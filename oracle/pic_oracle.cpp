@@ -202,6 +202,7 @@ struct Sim {
   double q[2], m[2], kt[2], dtin[2];
   double cb; /* fixed-point charge -> Jacobi source term, interior rows */
   std::vector<R> phi, ex, ey;
+  std::vector<double> phi64; /* F32 with refine_every > 0: the FP64 potential */
   std::vector<int64_t> acc;  /* F32: raw (unfolded) fixed-point charge */
   std::vector<double> accd;  /* F64: raw charge sum */
   bool acc_valid = false;
@@ -344,9 +345,91 @@ struct Sim {
     }
   }
 
+  bool refined() const { return p.refine_every > 0; }
+
+  /* k fixed Jacobi sweeps of x with source src, the operation order of
+   * solve() (no convergence test) */
+  void fixed_sweeps(std::vector<R> &x, const std::vector<R> &src, int k) const {
+    std::vector<R> nw(x);
+    for (int it = 0; it < k; ++it) {
+#pragma omp parallel for schedule(static)
+      for (int j = 1; j < nny - 1; ++j) {
+        const R *c = &x[(size_t)j * nnx];
+        const R *dn = c - nnx;
+        const R *up = c + nnx;
+        const R *bb = &src[(size_t)j * nnx];
+        R *o = &nw[(size_t)j * nnx];
+        for (int i = 0; i < nnx - 1; ++i) {
+          const R W = (i == 0) ? c[nnx - 2] : c[i - 1];
+          o[i] = (R)0.25 * ((((bb[i] + W) + c[i + 1]) + up[i]) + dn[i]);
+        }
+        o[nnx - 1] = o[0];
+      }
+      x.swap(nw);
+    }
+  }
+
+  /* Precision form (refine_every = m > 0).  F32: the GPU's algorithm step
+   * for step -- FP64 residual r = b - A phi64, m FP32 sweeps on the
+   * correction with source (float)r, FP64 update.  F64: plain FP64 Jacobi
+   * with the same stop rule (its iterates equal the F32 form's in exact
+   * arithmetic).  Stop when max|r| < tol after at least mn sweeps, or at mx
+   * sweeps; the residual is checked before every block of m sweeps. */
+  void solve_refined(double tol, int mn, int mx, int *sweeps, double *res) {
+    const size_t nn = (size_t)nnx * nny;
+    const int m = p.refine_every;
+    if (F32 && phi64.size() != nn) phi64.assign(phi.begin(), phi.end());
+    std::vector<double> b64(nn, 0.0);
+    for (int j = 1; j < nny - 1; ++j)
+      for (int i = 0; i < nnx; ++i)
+        b64[(size_t)j * nnx + i] =
+            F32 ? (double)folded_fixed(j, i) * cb : folded(j, i) / (p.ds * p.eps0);
+    std::vector<R> rr(nn, (R)0), src;
+    if (!F32) src.assign(b64.begin(), b64.end());
+    auto P = [&](size_t k) -> double { return F32 ? phi64[k] : (double)phi[k]; };
+    int s = 0;
+    double rmax = 0.0;
+    for (;;) {
+      rmax = 0.0;
+#pragma omp parallel for reduction(max : rmax) schedule(static)
+      for (int j = 1; j < nny - 1; ++j) {
+        const size_t rb = (size_t)j * nnx;
+        for (int i = 0; i < nnx; ++i) {
+          const int ii = i == nnx - 1 ? 0 : i;
+          const double c = P(rb + ii), w = P(rb + (ii == 0 ? nnx - 2 : ii - 1));
+          const double e = P(rb + ii + 1), n = P(rb + nnx + ii), so = P(rb - nnx + ii);
+          const double r = b64[rb + ii] - (4.0 * c - (((w + e) + n) + so));
+          rr[rb + i] = (R)r;
+          rmax = std::max(rmax, std::fabs(r));
+        }
+      }
+      if ((s >= mn && rmax < tol) || s >= mx) break;
+      const int k = std::min(m, mx - s);
+      if constexpr (F32) {
+        std::vector<R> dl(nn, (R)0);
+        fixed_sweeps(dl, rr, k);
+        for (int j = 1; j < nny - 1; ++j)
+          for (int i = 0; i < nnx; ++i) phi64[(size_t)j * nnx + i] += (double)dl[(size_t)j * nnx + i];
+        for (size_t q = 0; q < nn; ++q) phi[q] = (R)phi64[q];
+      } else {
+        fixed_sweeps(phi, src, k);
+      }
+      s += k;
+    }
+    if (sweeps) *sweeps = s;
+    if (res) *res = rmax;
+    st.sweeps = s;
+    st.residual = (float)rmax;
+  }
+
   /* ---- Jacobi: mesh.cu:327-369 (5-point stencil, periodic seam) ---------- */
   void solve(double tol, int min_s, int max_s, int check, int *sweeps, double *res) {
     if (!acc_valid) deposit();
+    if (refined()) {
+      rho_out(rho_used);
+      solve_refined(tol, min_s, max_s, sweeps, res);
+      return;
+    }
     rho_out(rho_used);
     std::vector<R> b((size_t)nnx * nny, (R)0);
     for (int j = 1; j < nny - 1; ++j)
@@ -398,6 +481,29 @@ struct Sim {
 
   /* ---- field: mesh.cu:413-468 ------------------------------------------ */
   void field() {
+    if (F32 && refined()) {  /* from the FP64 potential, rounded once */
+      const double ds_d = p.ds;
+#pragma omp parallel for schedule(static)
+      for (int j = 0; j < nny; ++j)
+        for (int i = 0; i < nnx; ++i) {
+          const size_t k = (size_t)j * nnx + i, r = (size_t)j * nnx;
+          double fx = 0.0, fy;
+          if (j == 0) {
+            fy = (phi64[k] - phi64[k + nnx]) / ds_d;
+          } else if (j == nny - 1) {
+            fy = (phi64[k - nnx] - phi64[k]) / ds_d;
+          } else {
+            const bool seam = i == 0 || i == nnx - 1;
+            const double W = seam ? phi64[r + nnx - 2] : phi64[k - 1];
+            const double E = seam ? phi64[r + 1] : phi64[k + 1];
+            fx = (W - E) / (2.0 * ds_d);
+            fy = (phi64[k - nnx] - phi64[k + nnx]) / (2.0 * ds_d);
+          }
+          ex[k] = (R)fx;
+          ey[k] = (R)fy;
+        }
+      return;
+    }
 #pragma omp parallel for schedule(static)
     for (int j = 0; j < nny; ++j) {
       for (int i = 0; i < nnx; ++i) {
@@ -602,9 +708,13 @@ struct Sim {
         }
       }
     }
+    if (F32 && refined()) phi64.assign((size_t)nnx * nny, 0.0);
     for (int j = 0; j < nny; ++j)
-      for (int i = 0; i < nnx; ++i)
-        phi[(size_t)j * nnx + i] = (R)((1.0 - (double)j / (double)ncy) * p.phi_p);
+      for (int i = 0; i < nnx; ++i) {
+        const double v = (1.0 - (double)j / (double)ncy) * p.phi_p;
+        phi[(size_t)j * nnx + i] = (R)v;
+        if (F32 && refined()) phi64[(size_t)j * nnx + i] = v;
+      }
     deposit();
     solve(p.init_tol, p.init_min_sweeps, p.init_max_sweeps, p.check_every, nullptr, nullptr);
     field();
@@ -909,6 +1019,10 @@ int ora_get_row_counts(void *h, int sp, int32_t *counts) {
 
 int ora_get_phi(void *h, double *o) {
   return dispatch(h, [&](auto &s) {
+    if (!s.phi64.empty()) {  // the precision form's FP64 potential
+      for (size_t k = 0; k < s.phi64.size(); ++k) o[k] = s.phi64[k];
+      return (int)CUPIC_OK;
+    }
     for (size_t k = 0; k < s.phi.size(); ++k) o[k] = (double)s.phi[k];
     return (int)CUPIC_OK;
   });
@@ -918,6 +1032,7 @@ int ora_set_phi(void *h, const double *v) {
   return dispatch(h, [&](auto &s) {
     using R = typename std::decay<decltype(s.phi[0])>::type;
     for (size_t k = 0; k < s.phi.size(); ++k) s.phi[k] = (R)v[k];
+    if (s.F32 && s.refined()) s.phi64.assign(v, v + s.phi.size());
     return (int)CUPIC_OK;
   });
 }

@@ -1,0 +1,146 @@
+"""The precision form of the Poisson solve (refine_every > 0), on the GPU.
+
+FP32 Jacobi sweeps solve for a correction; the residual b - A phi of the
+5-point operator, the update of the potential and the field are FP64.
+  bit-exact : against the FP32 oracle, which restates the same algorithm
+              (particles, phi, E, sweep counts, residuals)
+  <= 1e-9   : relative error of phi against a plain FP64 Jacobi run on the
+              same fixed-point charge with the same sweep count (E is stored
+              in FP32 for the push: <= 1e-7, one rounding); the FP32 solve of
+              the same problem is held to show its larger error
+  2%        : time-averaged probe current (net charge absorbed per step) and
+              density profile over the last 1000 of 2000 steps, against the
+              all-FP64 oracle running the same solve rule from the same seed
+"""
+import numpy as np
+import pytest
+
+import cupic_gb300 as cg
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def fp64_jacobi(p, acc, phi0, sweeps):
+    """Plain FP64 Jacobi of the 5-point operator (periodic x, Dirichlet y)
+    on the fixed-point charge acc, from phi0; the FP64 field of the result."""
+    nnx, nny = p.nnx, p.nny
+    a = acc.reshape(nny, nnx).astype(np.float64)
+    f = a.copy()
+    f[:, 0] = a[:, 0] + a[:, -1]
+    f[:, -1] = f[:, 0]
+    b = f * (2.0 ** -32 / (p.ds * p.eps0))
+    phi = phi0.reshape(nny, nnx).astype(np.float64).copy()
+    for _ in range(sweeps):
+        w = np.concatenate([phi[1:-1, -2:-1], phi[1:-1, :-2]], axis=1)
+        new = 0.25 * ((((b[1:-1, :-1] + w) + phi[1:-1, 1:]) + phi[2:, :-1]) + phi[:-2, :-1])
+        phi[1:-1, :-1] = new
+        phi[1:-1, -1] = new[:, 0]
+    ex = np.zeros_like(phi)
+    ey = np.zeros_like(phi)
+    wcol = np.concatenate([phi[:, -2:-1], phi[:, :-2], phi[:, -2:-1]], axis=1)
+    ecol = np.concatenate([phi[:, 1:], phi[:, 1:2]], axis=1)
+    ex[1:-1] = (wcol[1:-1] - ecol[1:-1]) / (2 * p.ds)
+    ey[1:-1] = (phi[:-2] - phi[2:]) / (2 * p.ds)
+    ey[0] = (phi[0] - phi[1]) / p.ds
+    ey[-1] = (phi[-2] - phi[-1]) / p.ds
+    return phi, ex, ey
+
+
+def linear_phi(p):
+    j = np.arange(p.nny, dtype=np.float64)[:, None]
+    return np.broadcast_to((1.0 - j / p.ncy) * p.phi_p, (p.nny, p.nnx)).copy()
+
+
+def rel(a, b):
+    return float(np.abs(np.asarray(a, np.float64) - b).max() / np.abs(b).max())
+
+
+@pytest.fixture
+def sims(gpu_lib):
+    made = []
+    yield made
+    for s in made:
+        s.close()
+
+
+def test_precision_form_matches_oracle_bit_for_bit(sims):
+    p = cg.workload_params("tiny", refine_every=8, tol=1e-10, min_sweeps=8, max_sweeps=200,
+                           init_tol=1e-10, init_min_sweeps=8, init_max_sweeps=800)
+    sim = cg.Sim(p)
+    sims.append(sim)
+    ora = Oracle(p, fp64=False)
+    sim.init_plasma()
+    ora.init_plasma()
+    np.testing.assert_array_equal(sim.phi64(), ora.phi())
+    for _ in range(4):
+        sim.step(1)
+        ora.step(1)
+        g, o = sim.stats(1)[0], ora.stats()
+        for k in ("absorbed", "removed", "injected", "live", "sweeps"):
+            assert g[k] == o[k], k
+        assert g["residual"] == o["residual"]
+    for sp in (0, 1):
+        np.testing.assert_array_equal(sim.particles(sp), ora.particles(sp))
+    np.testing.assert_array_equal(sim.phi64(), ora.phi())
+    exg, eyg = sim.efield()
+    exo, eyo = ora.efield()
+    np.testing.assert_array_equal(exg.astype(np.float64), exo)
+    np.testing.assert_array_equal(eyg.astype(np.float64), eyo)
+
+
+def test_precision_form_error_against_fp64(sims):
+    """phi and E of the precision form against FP64 Jacobi on the same
+    charge and sweep count, beside the FP32 solve's error."""
+    errs = {}
+    for m in (32, 0):
+        p = cg.workload_params("small", refine_every=m, init_tol=0.0, init_min_sweeps=1024,
+                               init_max_sweeps=1024, check_every=1024)
+        sim = cg.Sim(p)
+        sims.append(sim)
+        sim.init_plasma()  # linear phi, deposit, 1024 sweeps, field
+        ref, exr, eyr = fp64_jacobi(p, sim.rho_fixed(0).ravel(), linear_phi(p), 1024)
+        phi = sim.phi64() if m else sim.phi().astype(np.float64)
+        ex, ey = sim.efield()
+        errs[m] = (rel(phi, ref), rel(ex, exr), rel(ey, eyr))
+    print(f"\nrelative error vs FP64 Jacobi (phi, Ex, Ey): precision form {errs[32]}, FP32 {errs[0]}")
+    assert errs[32][0] <= 1e-9
+    assert max(errs[32][1:]) <= 1e-7
+    assert errs[0][0] > 100 * errs[32][0]
+
+
+def test_probe_current_and_density_within_2pct_of_fp64(sims):
+    """2000 steps of a 256x64-cell plasma (20 particles per cell per
+    species) in the precision form against the all-FP64 oracle with the same
+    solve rule.  The probe current is the net charge absorbed per step (ions
+    minus electrons); the density profile is the electron count in 16 bins
+    of y.  Both are averaged over the last 1000 steps."""
+    p = cg.workload_params("small", ncx=256, ncy=64, refine_every=32, tol=4e-6, min_sweeps=32,
+                           max_sweeps=512, init_tol=4e-6, init_min_sweeps=32,
+                           init_max_sweeps=20000, check_every=32)
+    steps, window, bins = 2000, 1000, 16
+    sim = cg.Sim(p)
+    sims.append(sim)
+    sim.init_plasma()
+    ora = Oracle(p, fp64=True)
+    ora.init_plasma()
+    cur_g, cur_o = [], []
+    prof_g = np.zeros(bins)
+    prof_o = np.zeros(bins)
+    for k in range(steps):
+        sim.step(1)
+        ora.step(1)
+        g, o = sim.stats(1)[0], ora.stats()
+        assert g["flags"] == 0
+        if k >= steps - window:
+            cur_g.append(g["absorbed"][1] - g["absorbed"][0])
+            cur_o.append(o["absorbed"][1] - o["absorbed"][0])
+            prof_g += sim.row_counts(0).reshape(bins, -1).sum(1)
+            prof_o += ora.row_counts(0).reshape(bins, -1).sum(1)
+    ig, io = np.mean(cur_g), np.mean(cur_o)
+    bulk = prof_o[bins // 2:].mean()
+    dev = np.abs(prof_g - prof_o).max() / bulk
+    print(f"\nprobe current (net charge absorbed per step): GPU {ig:.3f}, FP64 oracle {io:.3f}, "
+          f"diff {abs(ig - io) / io:.4f}; density profile max deviation {dev:.4f} of bulk")
+    assert abs(ig - io) <= 0.02 * io
+    assert dev <= 0.02
