@@ -17,7 +17,8 @@ from .params import Params, StepStats, workload_params
 __all__ = ["Sim", "Params", "StepStats", "workload_params", "load_library", "library_path",
            "CupicError", "params_from_input_data", "SPECIES", "FLAGS", "EXPORTED",
            "write_particles_file", "read_particles_file", "write_mesh_file",
-           "write_bookmarks_file", "write_bins_file", "rewrite_input_data", "driver_path"]
+           "write_bookmarks_file", "write_bins_file", "rewrite_input_data", "driver_path",
+           "Batch"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
@@ -40,6 +41,8 @@ EXPORTED = [
     "cupic_read_particles_file", "cupic_write_mesh_file", "cupic_write_bookmarks_file",
     "cupic_write_bins_file", "cupic_rewrite_input_data", "cupic_particles_snapshot",
     "cupic_mesh_snapshot", "cupic_save_bm", "cupic_save_bins", "cupic_load_particles_file",
+    "cupic_batch_create", "cupic_batch_set", "cupic_batch_step", "cupic_batch_sync",
+    "cupic_batch_destroy",
 ]
 
 
@@ -122,6 +125,11 @@ def load_library(build_if_missing=False):
         "cupic_save_bm": [vp, c_i, ctypes.c_char_p],
         "cupic_save_bins": [vp, c_i, ctypes.c_char_p],
         "cupic_load_particles_file": [vp, c_i, ctypes.c_char_p],
+        "cupic_batch_create": [c_i, P(vp)],
+        "cupic_batch_set": [vp, P(vp), c_i32],
+        "cupic_batch_step": [vp, c_i32],
+        "cupic_batch_sync": [vp],
+        "cupic_batch_destroy": [vp],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -397,3 +405,49 @@ class Sim:
 
     def save_bins(self, species, path):
         _ok(self.L.cupic_save_bins(self.h, species, os.fsencode(path)), "save_bins")
+
+
+class Batch:
+    """Many contexts stepped together (cupic_batch_*): one launch per kernel
+    for all members.  Step members only through the batch while they are
+    members, and sync before reading them."""
+
+    def __init__(self, sims=(), device=0):
+        self.L = load_library()
+        h = ctypes.c_void_p()
+        _ok(self.L.cupic_batch_create(device, ctypes.byref(h)), "cupic_batch_create")
+        self.h = h
+        self.sims = []
+        if sims:
+            self.set(sims)
+
+    def set(self, sims):
+        sims = list(sims)
+        arr = (ctypes.c_void_p * max(len(sims), 1))(*[s.h.value for s in sims])
+        _ok(self.L.cupic_batch_set(self.h, arr, len(sims)), "batch_set")
+        self.sims = sims
+
+    def step(self, n=1, sync=True):
+        _ok(self.L.cupic_batch_step(self.h, n), "batch_step")
+        if sync:
+            self.sync()
+
+    def sync(self):
+        _ok(self.L.cupic_batch_sync(self.h), "batch_sync")
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.cupic_batch_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -18,7 +18,8 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libcupic_gpu.so")
 EXE = os.path.join(OUT, "cupic_run")
 REF_LIB = os.path.join(OUT, "libcupic_ref.so")
-SOURCES = ["capi.cu", "particles.cu", "jacobi.cu", "io.cu", "noalloc.cu", "refine.cu", "files.cpp"]
+SOURCES = ["capi.cu", "particles.cu", "jacobi.cu", "io.cu", "noalloc.cu", "refine.cu", "batch.cu",
+           "files.cpp"]
 MAIN = "cupic_main.cpp"
 REF_API = "ref_api.cpp"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -1,0 +1,409 @@
+// batch.cu -- many independent contexts (probe-bias instances of uneven
+// sizes) stepped together.  It has no counterpart in the reference, which
+// runs one simulation per process.
+//
+// One batched step is one launch per kernel for all members:
+//   - the solves: one cooperative launch whose CTAs are split into groups;
+//     a group of G CTAs solves its list of instances one after another
+//     (instances that fit one CTA's shared memory get G = 1, larger ones the
+//     fewest CTAs that hold them), groups sized and filled by the members'
+//     mesh work (largest first onto the least-loaded group);
+//   - push, arrive and the charge clear: work lists of {instance, row};
+//   - the injection draws (beside the push, on a side stream), the append
+//     and the bookkeeping: one block or thread per instance and species.
+// Every kernel reads its instance's SimArgs from a device array, so members
+// keep their own buffers and control blocks, and a member's results are the
+// ones it gets when stepped alone.  The step is captured once per
+// membership as a CUDA graph.
+#include <string.h>
+
+#include <algorithm>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "ctx.h"
+#include "kernels.h"
+
+using namespace cupic;
+
+struct cupic_batch {
+  int device = 0, num_sms = 0;
+  cudaStream_t stream = nullptr, side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  std::vector<cupic_ctx *> members;
+  // device arrays, grown as needed
+  SimArgs *d_inst = nullptr;
+  JacobiArgs *d_jargs = nullptr;
+  JGroup *d_groups = nullptr;
+  int *d_list = nullptr;
+  int2 *d_rows = nullptr, *d_nodes = nullptr;
+  unsigned *d_flags = nullptr;
+  float *d_res = nullptr, *d_halo = nullptr;
+  size_t cap_inst = 0, cap_groups = 0, cap_rows = 0, cap_nodes = 0, cap_flags = 0, cap_res = 0,
+         cap_halo = 0;
+  int ngroups = 0, nctas = 0, nrows = 0, nnodes = 0, max_nnx = 0, max_ncy = 0, max_inj = 0;
+  size_t nflags = 0, jsmem = 0;
+  cudaGraphExec_t graph = nullptr;
+  bool graph_ok = false;
+};
+
+namespace {
+
+#define CU(call)                                                            \
+  do {                                                                      \
+    cudaError_t e_ = (call);                                                \
+    if (e_ != cudaSuccess) return e_ == cudaErrorMemoryAllocation ? CUPIC_ERR_NOMEM \
+                                                                  : CUPIC_ERR_CUDA; \
+  } while (0)
+
+template <class T>
+int grow(T **p, size_t *cap, size_t n) {
+  if (n <= *cap && *p) return CUPIC_OK;
+  cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  const size_t m = std::max<size_t>(n, 1);
+  CU(cudaMalloc((void **)p, m * sizeof(T)));
+  *cap = m;
+  return CUPIC_OK;
+}
+
+void drop_graph(cupic_batch *b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  b->graph_ok = false;
+}
+
+// the batched solve's layout of one instance: the fewest CTAs whose shared
+// memory holds its rows, with a halo depth of up to 8
+struct Plan {
+  int G, B, K, P;
+  size_t smem;
+};
+
+bool plan_instance(const SimArgs &a, long long rows_fit, Plan *out) {
+  const int M = a.nny - 2;
+  const int P = (a.nnx + 3) / 4 * 4;
+  if (M + 2 <= rows_fit) {
+    *out = {1, M, 1, P, jacobi_smem_bytes(M, 1, P)};
+    return true;
+  }
+  for (int G = 2; G <= M; ++G) {
+    const int B = (M + G - 1) / G;
+    const int K = std::min(8, M / G);
+    if (K >= 1 && B + 2 * K <= rows_fit) {
+      *out = {G, B, K, P, jacobi_smem_bytes(B, K, P)};
+      return true;
+    }
+  }
+  return false;
+}
+
+int build(cupic_batch *b) {
+  drop_graph(b);
+  const int n = (int)b->members.size();
+  if (n == 0) return CUPIC_OK;
+  int dev_max = 0;
+  CU(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device));
+  std::vector<SimArgs> inst(n);
+  std::vector<Plan> plan(n);
+  std::vector<double> work(n);
+  size_t smem = 0;
+  b->max_nnx = b->max_ncy = b->max_inj = 0;
+  for (int i = 0; i < n; ++i) {
+    const cupic_ctx *c = b->members[i];
+    inst[i] = c->a;
+    const long long P = (c->a.nnx + 3) / 4 * 4;
+    const long long rows_fit = (long long)((dev_max - 1024) / (3 * sizeof(float) * P));
+    if (!plan_instance(c->a, rows_fit, &plan[i])) return CUPIC_ERR_ARG;
+    smem = std::max(smem, plan[i].smem);
+    work[i] = (double)c->a.nnx * c->a.nny * std::max(c->p.max_sweeps, 1);
+    b->max_nnx = std::max(b->max_nnx, c->a.nnx);
+    b->max_ncy = std::max(b->max_ncy, c->a.ncy);
+    b->max_inj = std::max({b->max_inj, c->a.sp[0].inj_cap, c->a.sp[1].inj_cap});
+  }
+  CU(jacobi_batch_set_smem(smem));
+  int per_sm = 0;
+  CU(jacobi_batch_max_ctas(smem, &per_sm));
+  const int T = per_sm * b->num_sms;
+  // buckets of equal CTA count; groups per bucket by work share
+  std::vector<int> sizes;
+  for (const Plan &q : plan) sizes.push_back(q.G);
+  std::sort(sizes.begin(), sizes.end());
+  sizes.erase(std::unique(sizes.begin(), sizes.end()), sizes.end());
+  const int nb = (int)sizes.size();
+  std::vector<double> bw(nb, 0.0);
+  std::vector<int> bcount(nb, 0), ng(nb, 1);
+  std::vector<int> bucket(n);
+  for (int i = 0; i < n; ++i) {
+    bucket[i] = (int)(std::lower_bound(sizes.begin(), sizes.end(), plan[i].G) - sizes.begin());
+    bw[bucket[i]] += work[i];
+    bcount[bucket[i]]++;
+  }
+  const double wtot = std::accumulate(bw.begin(), bw.end(), 0.0);
+  int used = 0;
+  for (int k = 0; k < nb; ++k) {
+    ng[k] = std::max(1, std::min(bcount[k], (int)(T * bw[k] / wtot / sizes[k])));
+    used += ng[k] * sizes[k];
+  }
+  while (used > T) {  // give back groups where a group carries the least work
+    int kk = -1;
+    for (int k = 0; k < nb; ++k)
+      if (ng[k] > 1 && (kk < 0 || bw[k] / ng[k] < bw[kk] / ng[kk])) kk = k;
+    if (kk < 0) return CUPIC_ERR_CAPACITY;  // one group per size does not fit the GPU
+    ng[kk]--;
+    used -= sizes[kk];
+  }
+  for (;;) {  // hand out the CTAs left where a group carries the most work
+    int kk = -1;
+    for (int k = 0; k < nb; ++k)
+      if (ng[k] < bcount[k] && used + sizes[k] <= T && (kk < 0 || bw[k] / ng[k] > bw[kk] / ng[kk]))
+        kk = k;
+    if (kk < 0) break;
+    ng[kk]++;
+    used += sizes[kk];
+  }
+  // groups: consecutive CTAs; instances of a bucket go largest first to the
+  // least-loaded group of the bucket
+  std::vector<JGroup> groups;
+  std::vector<std::vector<int>> glist;
+  std::vector<double> gload;
+  int first = 0;
+  for (int k = 0; k < nb; ++k) {
+    const int g0 = (int)groups.size();
+    for (int q = 0; q < ng[k]; ++q) {
+      groups.push_back({first, sizes[k], 0, 0});
+      glist.emplace_back();
+      gload.push_back(0.0);
+      first += sizes[k];
+    }
+    std::vector<int> ids;
+    for (int i = 0; i < n; ++i)
+      if (bucket[i] == k) ids.push_back(i);
+    std::sort(ids.begin(), ids.end(), [&](int x, int y) { return work[x] > work[y]; });
+    for (int i : ids) {
+      int best = g0;
+      for (int g = g0; g < g0 + ng[k]; ++g)
+        if (gload[g] < gload[best]) best = g;
+      glist[best].push_back(i);
+      gload[best] += work[i];
+    }
+  }
+  std::vector<int> list;
+  for (size_t g = 0; g < groups.size(); ++g) {
+    groups[g].begin = (int)list.size();
+    list.insert(list.end(), glist[g].begin(), glist[g].end());
+    groups[g].end = (int)list.size();
+  }
+  b->ngroups = (int)groups.size();
+  b->nctas = first;
+  b->jsmem = smem;
+  // exchange buffers of every instance's solve, one pool each
+  size_t nflags = 0, nres = 0, nhalo = 0;
+  for (int i = 0; i < n; ++i) {
+    nflags += plan[i].G + 1;
+    nres += 2 * plan[i].G;
+    nhalo += (size_t)4 * plan[i].G * plan[i].K * plan[i].P;
+  }
+  int rc;
+  if ((rc = grow(&b->d_flags, &b->cap_flags, nflags)) || (rc = grow(&b->d_res, &b->cap_res, nres)) ||
+      (rc = grow(&b->d_halo, &b->cap_halo, nhalo)))
+    return rc;
+  b->nflags = nflags;
+  std::vector<JacobiArgs> jargs(n);
+  size_t of = 0, orr = 0, oh = 0;
+  for (int i = 0; i < n; ++i) {
+    const cupic_ctx *c = b->members[i];
+    const Plan &q = plan[i];
+    JacobiArgs J{};
+    J.tol = c->p.tol;
+    J.min_sweeps = c->p.min_sweeps;
+    J.max_sweeps = c->p.max_sweeps;
+    J.check_every = std::max(1, c->p.check_every);
+    J.G = q.G;
+    J.rows_per_cta = q.B;
+    J.depth = q.K;
+    J.pitch = q.P;
+    J.vec = ((c->a.nnx - 1) % 4 == 0) ? 1 : 0;
+    J.strip = jacobi_strip_rows(c->a.nnx, q.B + 2 * (q.G > 1 ? q.K : 1) - 2);
+    J.do_field = 1;
+    J.write_stats = 1;
+    J.flags = b->d_flags + of;
+    J.bar = J.flags + q.G;
+    J.res_cta = b->d_res + orr;
+    J.halo = b->d_halo + oh;
+    of += q.G + 1;
+    orr += 2 * q.G;
+    oh += (size_t)4 * q.G * q.K * q.P;
+    jargs[i] = J;
+  }
+  // work lists
+  std::vector<int2> rows, nodes;
+  for (int i = 0; i < n; ++i) {
+    for (int s = 0; s < inst[i].ncy; ++s) rows.push_back(make_int2(i, s));
+    for (int j = 0; j < inst[i].nny; ++j) nodes.push_back(make_int2(i, j));
+  }
+  b->nrows = (int)rows.size();
+  b->nnodes = (int)nodes.size();
+  if ((rc = grow(&b->d_inst, &b->cap_inst, (size_t)n)) ||
+      (rc = grow(&b->d_groups, &b->cap_groups, groups.size())) ||
+      (rc = grow(&b->d_rows, &b->cap_rows, rows.size())) ||
+      (rc = grow(&b->d_nodes, &b->cap_nodes, nodes.size())))
+    return rc;
+  // d_jargs and d_list share the instance capacity
+  static_assert(sizeof(JacobiArgs) >= sizeof(int), "");
+  cudaFree(b->d_jargs);
+  cudaFree(b->d_list);
+  b->d_jargs = nullptr;
+  b->d_list = nullptr;
+  CU(cudaMalloc(&b->d_jargs, n * sizeof(JacobiArgs)));
+  CU(cudaMalloc(&b->d_list, n * sizeof(int)));
+  CU(cudaMemcpy(b->d_inst, inst.data(), n * sizeof(SimArgs), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(b->d_jargs, jargs.data(), n * sizeof(JacobiArgs), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(b->d_groups, groups.data(), groups.size() * sizeof(JGroup), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(b->d_list, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(b->d_rows, rows.data(), rows.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(b->d_nodes, nodes.data(), nodes.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  return CUPIC_OK;
+}
+
+int enqueue(cupic_batch *b) {
+  const int n = (int)b->members.size();
+  cudaStream_t st = b->stream;
+  CU(cudaMemsetAsync(b->d_flags, 0, b->nflags * sizeof(unsigned), st));
+  CU(launch_jacobi_batch(b->d_inst, b->d_jargs, b->d_groups, b->ngroups, b->d_list, b->nctas,
+                         b->jsmem, st));
+  CU(cudaEventRecord(b->ev_fork, st));
+  CU(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
+  CU(launch_inject_draw_batch(b->d_inst, n, b->max_inj, b->side));
+  CU(cudaEventRecord(b->ev_join, b->side));
+  CU(launch_zero_next_rho_batch(b->d_inst, b->d_nodes, b->nnodes, st));
+  CU(launch_push_deposit_batch(b->d_inst, b->d_rows, b->nrows, b->max_nnx, st));
+  CU(launch_arrive_batch(b->d_inst, b->d_rows, b->nrows, st));
+  CU(cudaStreamWaitEvent(st, b->ev_join, 0));
+  CU(launch_inject_append_batch(b->d_inst, n, b->max_ncy, st));
+  CU(launch_finalize_batch(b->d_inst, n, st));
+  return CUPIC_OK;
+}
+
+int capture(cupic_batch *b) {
+  drop_graph(b);
+  cudaGraph_t g = nullptr;
+  CU(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  const int rc = enqueue(b);
+  cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+  if (rc || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    return CUPIC_OK;  // direct launches instead
+  }
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    b->graph = nullptr;
+    return CUPIC_OK;
+  }
+  b->graph_ok = true;
+  return CUPIC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cupic_batch_create(int device, cupic_batch **out) {
+  if (!out) return CUPIC_ERR_ARG;
+  *out = nullptr;
+  cupic_batch *b = new (std::nothrow) cupic_batch();
+  if (!b) return CUPIC_ERR_NOMEM;
+  b->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    cupic_batch_destroy(b);
+    return CUPIC_ERR_CUDA;
+  }
+  *out = b;
+  return CUPIC_OK;
+}
+
+int cupic_batch_set(cupic_batch *b, cupic_ctx *const *members, int32_t n) {
+  if (!b || n < 0 || (n > 0 && !members)) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(b->device));
+  CU(cudaStreamSynchronize(b->stream));
+  for (int i = 0; i < n; ++i) {
+    const cupic_ctx *c = members[i];
+    if (!c || c->device != b->device) return CUPIC_ERR_ARG;
+    if (!c->initialized || !c->rho_valid) return CUPIC_ERR_STATE;
+    if (c->p.refine_every > 0) return CUPIC_ERR_ARG;  // the precision form steps alone
+    for (int k = 0; k < i; ++k)
+      if (members[k] == c) return CUPIC_ERR_ARG;
+  }
+  for (int i = 0; i < n; ++i) CU(cudaStreamSynchronize(members[i]->stream));
+  b->members.assign(members, members + n);
+  return build(b);
+}
+
+int cupic_batch_step(cupic_batch *b, int32_t nsteps) {
+  if (!b || nsteps < 0) return CUPIC_ERR_ARG;
+  if (b->members.empty() || nsteps == 0) return CUPIC_OK;
+  CU(cudaSetDevice(b->device));
+  if (!b->graph_ok) {
+    int rc = capture(b);
+    if (rc) return rc;
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    if (b->graph_ok) {
+      CU(cudaGraphLaunch(b->graph, b->stream));
+    } else {
+      int rc = enqueue(b);
+      if (rc) return rc;
+    }
+  }
+  for (cupic_ctx *c : b->members) c->host_cur ^= (nsteps & 1);
+  return CUPIC_OK;
+}
+
+int cupic_batch_sync(cupic_batch *b) {
+  if (!b) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(b->device));
+  CU(cudaStreamSynchronize(b->stream));
+  int first = CUPIC_OK;
+  for (cupic_ctx *c : b->members) {
+    const int rc = cupic_ctx_finish(c);
+    if (rc && !first) first = rc;
+  }
+  return first;
+}
+
+int cupic_batch_destroy(cupic_batch *b) {
+  if (!b) return CUPIC_ERR_ARG;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  drop_graph(b);
+  cudaFree(b->d_inst);
+  cudaFree(b->d_jargs);
+  cudaFree(b->d_groups);
+  cudaFree(b->d_list);
+  cudaFree(b->d_rows);
+  cudaFree(b->d_nodes);
+  cudaFree(b->d_flags);
+  cudaFree(b->d_res);
+  cudaFree(b->d_halo);
+  if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_join) cudaEventDestroy(b->ev_join);
+  if (b->side) {
+    cudaStreamSynchronize(b->side);
+    cudaStreamDestroy(b->side);
+  }
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return CUPIC_OK;
+}
+
+}  // extern "C"

@@ -16,42 +16,10 @@
 #include <tuple>
 #include <vector>
 
-#include "cupic_internal.cuh"
+#include "ctx.h"
 #include "kernels.h"
 
 using namespace cupic;
-
-struct cupic_ctx {
-  cupic_params p;
-  int device = 0;
-  int num_sms = 0;
-  cudaStream_t stream = nullptr;
-  // side branch of a step: the injection draws run beside the push
-  cudaStream_t side = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
-  SimArgs a{};
-  Ctl *ctl = nullptr;
-  std::vector<int64_t> seg[2];
-  std::vector<int32_t> cap[2];
-  int64_t total_cap[2] = {0, 0};
-  // Jacobi geometry and exchange buffers
-  int jG = 1, jB = 1, jK = 1, jP = 0;
-  unsigned *jflags = nullptr;  // [G+1]: per-CTA sweep counters, then the barrier
-  float *jres = nullptr;
-  float *jhalo = nullptr;
-  // precision form of the solve (refine_every > 0): FP64 potential, FP32
-  // residual source and correction, the residual's max norm
-  double *phi64 = nullptr;
-  float *rr = nullptr, *dl = nullptr;
-  unsigned long long *maxr = nullptr;
-  void *h_pin = nullptr;  // pinned: [0] max-norm bits, [1] {sweeps, residual}
-  // graph of one step
-  cudaGraphExec_t graph = nullptr;
-  bool graph_ok = false;
-  bool initialized = false;
-  bool rho_valid = false;
-  int host_cur = 0;
-};
 
 namespace {
 
@@ -617,6 +585,8 @@ bool read_i(const char *path, int n, int *v) {
 }
 
 }  // namespace
+
+int cupic_ctx_finish(cupic_ctx *c) { return finish(c); }
 
 extern "C" {
 

@@ -97,6 +97,11 @@ struct JacobiArgs {
   const float *src;       // FP32 source per node; NULL: the charge accumulator a.rho[cur]
 };
 
+// a group of CTAs of the batched solve and its instances (list[begin..end))
+struct JGroup {
+  int32_t first, G, begin, end;
+};
+
 // ---------------------------------------------------------------------------
 // arithmetic shared by the kernels
 // ---------------------------------------------------------------------------

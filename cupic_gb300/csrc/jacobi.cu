@@ -224,10 +224,10 @@ __device__ __forceinline__ float sweep_reg(float4 (&x)[R], const float4 (&b)[R],
 // R > 0 selects the register-strip sweep with strips of R rows; R == 0 the
 // shared-memory sweep (sweep_vec / sweep_scalar).
 template <int R>
-__device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &J, float *jsm, float *red,
-                                            int *bail_p) {
+__device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &J, const int c, float *jsm,
+                                            float *red, int *bail_p) {
   int &bail = *bail_p;
-  const int c = blockIdx.x, G = J.G, tid = threadIdx.x;
+  const int G = J.G, tid = threadIdx.x;
   const int nnx = a.nnx, nny = a.nny, P = J.pitch;
   const int M = nny - 2;
   const int K = G > 1 ? J.depth : 1;
@@ -461,18 +461,48 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
   }
 }
 
+__device__ __forceinline__ void jacobi_dispatch(const SimArgs &a, const JacobiArgs &J, int c, float *jsm,
+                                                float *red, int *bail) {
+  switch (J.strip) {
+    case 1: jacobi_body<1>(a, J, c, jsm, red, bail); break;
+    case 2: jacobi_body<2>(a, J, c, jsm, red, bail); break;
+    case 4: jacobi_body<4>(a, J, c, jsm, red, bail); break;
+    case 8: jacobi_body<8>(a, J, c, jsm, red, bail); break;
+    default: jacobi_body<0>(a, J, c, jsm, red, bail); break;
+  }
+}
+
 __global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) {
   extern __shared__ __align__(16) float jsm[];
   __shared__ float red[33];
   __shared__ int bail;
   if (threadIdx.x == 0) bail = 0;
   __syncthreads();
-  switch (J.strip) {
-    case 1: jacobi_body<1>(a, J, jsm, red, &bail); break;
-    case 2: jacobi_body<2>(a, J, jsm, red, &bail); break;
-    case 4: jacobi_body<4>(a, J, jsm, red, &bail); break;
-    case 8: jacobi_body<8>(a, J, jsm, red, &bail); break;
-    default: jacobi_body<0>(a, J, jsm, red, &bail); break;
+  jacobi_dispatch(a, J, blockIdx.x, jsm, red, &bail);
+}
+
+// Many contexts' solves in one cooperative launch.  The grid is split into
+// groups of CTAs; group g (CTAs first .. first+G-1) solves the instances
+// list[begin .. end) one after another, its CTA c acting as CTA c of each
+// solve.  The instances of a group share its CTA count; their exchange
+// flags are zeroed before the launch.
+__global__ void __launch_bounds__(kJBlock, 1)
+    k_jacobi_batch(const SimArgs *__restrict__ inst, const JacobiArgs *__restrict__ jargs,
+                   const JGroup *__restrict__ groups, int ngroups, const int *__restrict__ list) {
+  extern __shared__ __align__(16) float jsm[];
+  __shared__ float red[33];
+  __shared__ int bail;
+  int g = 0;
+  while (g + 1 < ngroups && groups[g + 1].first <= (int)blockIdx.x) ++g;
+  const JGroup gr = groups[g];
+  const int c = (int)blockIdx.x - gr.first;
+  if (c < 0 || c >= gr.G) return;
+  for (int q = gr.begin; q < gr.end; ++q) {
+    const int i = list[q];
+    if (threadIdx.x == 0) bail = 0;
+    __syncthreads();
+    jacobi_dispatch(inst[i], jargs[i], c, jsm, red, &bail);
+    __syncthreads();
   }
 }
 
@@ -505,6 +535,34 @@ cudaError_t jacobi_set_smem(size_t bytes) {
 
 cudaError_t jacobi_max_ctas(size_t smem, int *per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_jacobi, kJBlock, smem);
+}
+
+cudaError_t jacobi_batch_set_smem(size_t bytes) {
+  static size_t cur = 48 * 1024;
+  if (bytes <= cur) return cudaSuccess;
+  cudaError_t e =
+      cudaFuncSetAttribute(k_jacobi_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) cur = bytes;
+  return e;
+}
+
+cudaError_t jacobi_batch_max_ctas(size_t smem, int *per_sm) {
+  return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_jacobi_batch, kJBlock, smem);
+}
+
+cudaError_t launch_jacobi_batch(const SimArgs *inst, const JacobiArgs *jargs, const JGroup *groups,
+                                int ngroups, const int *list, int nctas, size_t smem, cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nctas);
+  cfg.blockDim = dim3(kJBlock);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_jacobi_batch, inst, jargs, groups, ngroups, list);
 }
 
 cudaError_t launch_jacobi(const SimArgs &a, const JacobiArgs &J, cudaStream_t st) {

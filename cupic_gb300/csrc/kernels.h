@@ -37,6 +37,21 @@ cudaError_t jacobi_set_smem(size_t bytes);
 cudaError_t jacobi_max_ctas(size_t smem, int *per_sm);
 cudaError_t launch_jacobi(const SimArgs &a, const JacobiArgs &J, cudaStream_t st);
 
+// many contexts in one launch (batch.cu): SimArgs / JacobiArgs arrays in
+// device memory, work lists of {instance, row}
+cudaError_t jacobi_batch_set_smem(size_t bytes);
+cudaError_t jacobi_batch_max_ctas(size_t smem, int *per_sm);
+cudaError_t launch_jacobi_batch(const SimArgs *inst, const JacobiArgs *jargs, const JGroup *groups,
+                                int ngroups, const int *list, int nctas, size_t smem, cudaStream_t st);
+cudaError_t launch_zero_next_rho_batch(const SimArgs *inst, const int2 *node_work, int n,
+                                       cudaStream_t st);
+cudaError_t launch_push_deposit_batch(const SimArgs *inst, const int2 *row_work, int n, int max_nnx,
+                                      cudaStream_t st);
+cudaError_t launch_arrive_batch(const SimArgs *inst, const int2 *row_work, int n, cudaStream_t st);
+cudaError_t launch_inject_draw_batch(const SimArgs *inst, int n, int max_inj_cap, cudaStream_t st);
+cudaError_t launch_inject_append_batch(const SimArgs *inst, int n, int max_ncy, cudaStream_t st);
+cudaError_t launch_finalize_batch(const SimArgs *inst, int n, cudaStream_t st);
+
 // precision form of the solve (refine.cu)
 cudaError_t launch_r64_residual(const SimArgs &a, const double *phi64, float *rr, float *dl,
                                 unsigned long long *maxr, cudaStream_t st);

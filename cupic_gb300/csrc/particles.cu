@@ -263,11 +263,10 @@ size_t push_smem_bytes(int nnx) {
          (size_t)2 * nnx * sizeof(float2);
 }
 
-__global__ void __launch_bounds__(kPB, 3) k_push_deposit(SimArgs a) {
-  extern __shared__ __align__(128) unsigned char push_raw[];
+__device__ __forceinline__ void push_row(const SimArgs &a, const int s, unsigned char *push_raw) {
   constexpr int NW = kPB / 32;
   constexpr int NE = kNE;  // scan entries per chunk, (j, warp) in j-major order
-  const int s = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nnx = a.nnx;
   const int ncx = a.ncx;
   float4 *stage = reinterpret_cast<float4 *>(push_raw);
@@ -443,11 +442,23 @@ __global__ void __launch_bounds__(kPB, 3) k_push_deposit(SimArgs a) {
   if (lane == 0) raise_flags(ctl, fl);
 }
 
+__global__ void __launch_bounds__(kPB, 3) k_push_deposit(SimArgs a) {
+  extern __shared__ __align__(128) unsigned char push_raw[];
+  push_row(a, blockIdx.x, push_raw);
+}
+
+// many contexts in one launch: work[b] = {instance, row}
+__global__ void __launch_bounds__(kPB, 3)
+    k_push_deposit_batch(const SimArgs *__restrict__ inst, const int2 *__restrict__ work) {
+  extern __shared__ __align__(128) unsigned char push_raw[];
+  const int2 w = work[blockIdx.x];
+  push_row(inst[w.x], w.y, push_raw);
+}
+
 // ---------------------------------------------------------------------------
 // append the movers: row d = [stayed] + [up from d-1] + [down from d+1]
 // ---------------------------------------------------------------------------
-__global__ void k_arrive(SimArgs a) {
-  const int d = blockIdx.x, sp = blockIdx.y;
+__device__ __forceinline__ void arrive_row(const SimArgs &a, const int d, const int sp) {
   const SpeciesDev &S = a.sp[sp];
   const int ns = S.nstay[d];
   const int nb = d > 0 ? S.nup[d - 1] : 0;
@@ -471,6 +482,13 @@ __global__ void k_arrive(SimArgs a) {
   }
 }
 
+__global__ void k_arrive(SimArgs a) { arrive_row(a, blockIdx.x, blockIdx.y); }
+
+__global__ void k_arrive_batch(const SimArgs *__restrict__ inst, const int2 *__restrict__ work) {
+  const int2 w = work[blockIdx.x];
+  arrive_row(inst[w.x], w.y, blockIdx.y);
+}
+
 // ---------------------------------------------------------------------------
 // injection of the half-Maxwellian flux at y = Ly (cc.cu:179-256), in three
 // kernels:
@@ -482,9 +500,7 @@ __global__ void k_arrive(SimArgs a) {
 //   k_inject_append  one block per species: stable rank of each draw within
 //                    its destination row, append, deposit
 // ---------------------------------------------------------------------------
-__global__ void k_inject_sched(SimArgs a) {
-  const int sp = threadIdx.x;
-  if (sp > 1) return;
+__device__ __forceinline__ void inject_sched(const SimArgs &a, const int sp) {
   const SpeciesDev &S = a.sp[sp];
   Ctl *ctl = a.ctl;
   const double t = ctl->t;
@@ -507,9 +523,17 @@ __global__ void k_inject_sched(SimArgs a) {
   ctl->inj_gen[sp] = ne;
 }
 
-__global__ void k_inject_gen(SimArgs a) {
-  const int sp = blockIdx.y;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void k_inject_sched(SimArgs a) {
+  if (threadIdx.x < 2) inject_sched(a, threadIdx.x);
+}
+
+// thread 2*i + sp handles species sp of instance i
+__global__ void k_inject_sched_batch(const SimArgs *__restrict__ inst, int n) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t < 2 * n) inject_sched(inst[t >> 1], t & 1);
+}
+
+__device__ __forceinline__ void inject_gen(const SimArgs &a, const int sp, const int k) {
   const Ctl *ctl = a.ctl;
   const int ne = ctl->inj_gen[sp];
   if (k >= ne) return;
@@ -545,10 +569,19 @@ __global__ void k_inject_gen(SimArgs a) {
   S.inj_d[k] = c.dest;
 }
 
-__global__ void __launch_bounds__(kInjBlock) k_inject_append(SimArgs a) {
-  extern __shared__ int running[];  // [ncy] injected per destination row
+__global__ void k_inject_gen(SimArgs a) {
+  inject_gen(a, blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+// grid (draw blocks, species, instance)
+__global__ void k_inject_gen_batch(const SimArgs *__restrict__ inst) {
+  inject_gen(inst[blockIdx.z], blockIdx.y, blockIdx.x * blockDim.x + threadIdx.x);
+}
+
+__device__ __forceinline__ void inject_append(const SimArgs &a, const int sp, int *running) {
+  // running: [ncy] injected per destination row
   constexpr int NW = kInjBlock / 32;
-  const int sp = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const SpeciesDev &S = a.sp[sp];
   Ctl *ctl = a.ctl;
   __shared__ unsigned s_rem;
@@ -608,10 +641,21 @@ __global__ void __launch_bounds__(kInjBlock) k_inject_append(SimArgs a) {
   if (tid == 0 && s_rem) atomicAdd(&ctl->removed[sp], (unsigned long long)s_rem);
 }
 
+__global__ void __launch_bounds__(kInjBlock) k_inject_append(SimArgs a) {
+  extern __shared__ int running[];
+  inject_append(a, blockIdx.x, running);
+}
+
+// grid (species, instance)
+__global__ void __launch_bounds__(kInjBlock) k_inject_append_batch(const SimArgs *__restrict__ inst) {
+  extern __shared__ int running[];
+  inject_append(inst[blockIdx.y], blockIdx.x, running);
+}
+
 // ---------------------------------------------------------------------------
 // end of step: stats ring entry, clocks, charge buffer flip
 // ---------------------------------------------------------------------------
-__global__ void k_finalize(SimArgs a) {
+__device__ __forceinline__ void finalize(const SimArgs &a) {
   Ctl *ctl = a.ctl;
   __shared__ unsigned long long live[2];
   if (threadIdx.x < 2) live[threadIdx.x] = 0ull;
@@ -644,6 +688,18 @@ __global__ void k_finalize(SimArgs a) {
     ctl->step = ctl->step + 1;
     ctl->cur ^= 1;
   }
+}
+
+__global__ void k_finalize(SimArgs a) { finalize(a); }
+
+__global__ void k_finalize_batch(const SimArgs *__restrict__ inst) { finalize(inst[blockIdx.x]); }
+
+// work[b] = {instance, node row}
+__global__ void k_zero_next_rho_batch(const SimArgs *__restrict__ inst, const int2 *__restrict__ work) {
+  const int2 w = work[blockIdx.x];
+  const SimArgs &a = inst[w.x];
+  unsigned long long *r = a.rho[a.ctl->cur ^ 1] + (size_t)w.y * a.nnx;
+  for (int i = threadIdx.x; i < a.nnx; i += blockDim.x) r[i] = 0ull;
 }
 
 // ---------------------------------------------------------------------------
@@ -713,6 +769,49 @@ cudaError_t launch_inject(const SimArgs &a, cudaStream_t st) {
   cudaError_t e = launch_inject_draw(a, st);
   if (e != cudaSuccess) return e;
   return launch_inject_append(a, st);
+}
+
+cudaError_t launch_zero_next_rho_batch(const SimArgs *inst, const int2 *node_work, int n,
+                                       cudaStream_t st) {
+  k_zero_next_rho_batch<<<n, 256, 0, st>>>(inst, node_work);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_push_deposit_batch(const SimArgs *inst, const int2 *row_work, int n, int max_nnx,
+                                      cudaStream_t st) {
+  static size_t cur = 48 * 1024;  // the attribute only grows
+  const size_t sm = push_smem_bytes(max_nnx);
+  if (sm > cur) {
+    cudaError_t e = cudaFuncSetAttribute(k_push_deposit_batch,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    cur = sm;
+  }
+  k_push_deposit_batch<<<n, kPB, sm, st>>>(inst, row_work);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_arrive_batch(const SimArgs *inst, const int2 *row_work, int n, cudaStream_t st) {
+  k_arrive_batch<<<dim3(n, 2), 128, 0, st>>>(inst, row_work);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_inject_draw_batch(const SimArgs *inst, int n, int max_inj_cap, cudaStream_t st) {
+  k_inject_sched_batch<<<(2 * n + 127) / 128, 128, 0, st>>>(inst, n);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_inject_gen_batch<<<dim3((max_inj_cap + 127) / 128, 2, n), 128, 0, st>>>(inst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_inject_append_batch(const SimArgs *inst, int n, int max_ncy, cudaStream_t st) {
+  k_inject_append_batch<<<dim3(2, n), kInjBlock, max_ncy * sizeof(int), st>>>(inst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_finalize_batch(const SimArgs *inst, int n, cudaStream_t st) {
+  k_finalize_batch<<<n, 256, 0, st>>>(inst);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_finalize(const SimArgs &a, cudaStream_t st) {

@@ -259,6 +259,27 @@ int cupic_poisson_solver_static(const cupic_params *p, const int64_t *rho_dev, f
                                 int32_t max_sweeps, int32_t check_every, void *stream,
                                 int32_t *sweeps_out, float *residual_out);
 
+/* ---- batched form ------------------------------------------------------- */
+/* Many independent contexts (probe-bias instances of any sizes) stepped
+ * together.  It has no counterpart in the reference, which runs one
+ * simulation per process.  A batched step is one launch per kernel for all
+ * members: the solves run in one cooperative launch of CTA groups, each
+ * group solving its list of instances in turn; push, arrive and the charge
+ * clear run over work lists of {instance, row}.  Each member keeps its own
+ * buffers, clocks and stats ring, and gets the same results as when stepped
+ * alone.  Members must be initialised contexts of the batch's device in the
+ * FP32 solve form; while they are members, step them only through the
+ * batch, and call cupic_batch_sync before reading them. */
+typedef struct cupic_batch cupic_batch;
+int cupic_batch_create(int device, cupic_batch **out);
+/* Sets the members (replacing the previous set); n == 0 empties the batch. */
+int cupic_batch_set(cupic_batch *b, struct cupic_ctx *const *members, int32_t n);
+/* nsteps batched cycles, replayed from a CUDA graph captured per member set. */
+int cupic_batch_step(cupic_batch *b, int32_t nsteps);
+/* Waits for the batch; returns the first member's error status, if any. */
+int cupic_batch_sync(cupic_batch *b);
+int cupic_batch_destroy(cupic_batch *b);
+
 /* ---- the reference's text files ---------------------------------------- */
 /* Host-side only; paths are used as given (the reference's ".dat" suffix
  * and "../output/" prefix are the caller's).  The formats are the

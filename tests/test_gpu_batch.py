@@ -1,0 +1,88 @@
+"""The batched form (cupic_batch_*) on the GPU.
+
+Contexts of uneven sizes stepped together in one launch per kernel must
+give, bit for bit, what each gets when stepped alone: particles (order
+included), phi, E and every per-step counter.  One member is large enough
+that its solve takes a group of many CTAs inside the batched launch.
+"""
+import numpy as np
+import pytest
+
+import cupic_gb300 as cg
+
+pytestmark = pytest.mark.gpu
+
+FIXED = dict(tol=0.0, check_every=100, min_sweeps=100, max_sweeps=100, init_tol=0.0,
+             init_min_sweeps=100, init_max_sweeps=100)
+MEMBERS = [
+    ("tiny", {}),
+    ("tiny", dict(seed=11, phi_p=2.0)),
+    ("small", dict(ncx=32, ncy=128, n=40.0, eps0=40.0, seed=3, **FIXED)),
+    ("small", dict(ncx=64, ncy=256, n=80.0, eps0=80.0, seed=4, mi=1836.0, kti=0.1, **FIXED)),
+    ("small", dict(ncx=256, ncy=1024, n=40.0, eps0=40.0, seed=5, phi_p=-10.0, **FIXED)),
+]
+
+
+def make_all():
+    out = []
+    for name, over in MEMBERS:
+        s = cg.Sim(cg.workload_params(name, **over))
+        s.init_plasma()
+        out.append(s)
+    return out
+
+
+def compare(a, b, what):
+    for sp in (0, 1):
+        np.testing.assert_array_equal(a.particles(sp), b.particles(sp), err_msg=f"{what} species {sp}")
+    np.testing.assert_array_equal(a.phi(), b.phi(), err_msg=f"{what} phi")
+    for x, y in zip(a.efield(), b.efield()):
+        np.testing.assert_array_equal(x, y, err_msg=f"{what} E")
+    np.testing.assert_array_equal(a.rho_fixed(0), b.rho_fixed(0), err_msg=f"{what} rho")
+
+
+def test_batch_equals_members_alone(gpu_lib):
+    alone, batched = make_all(), make_all()
+    steps = 6
+    try:
+        for s in alone:
+            s.step(steps)
+        with cg.Batch(batched) as b:
+            b.step(2)
+            b.step(steps - 2)
+        for k, (a, m) in enumerate(zip(alone, batched)):
+            compare(a, m, f"member {k}")
+            assert a.stats(steps) == m.stats(steps), f"member {k} stats"
+            assert m.flags() == 0
+    finally:
+        for s in alone + batched:
+            s.close()
+
+
+def test_membership_changes_between_steps(gpu_lib):
+    """Members leave and join between batched steps (continuous batching);
+    each one's state still equals its solo run."""
+    batched = make_all()
+    try:
+        with cg.Batch(batched[:2]) as b:
+            b.step(1)
+            b.set(batched[:4])       # two join
+            b.step(1)
+            b.set(batched[1:])       # one leaves, the large one joins
+            b.step(1)
+            b.set([batched[4], batched[2]])
+            b.step(1)
+            b.set([batched[3], batched[4]])
+            b.step(1)
+            b.set([batched[4]])
+            b.step(2)
+        # steps taken: member0 2, member1 3, member2 3, member3 3, member4 5
+        for k, n in enumerate((2, 3, 3, 3, 5)):
+            ref = cg.Sim(batched[k].p)
+            ref.init_plasma()
+            ref.step(n)
+            compare(ref, batched[k], f"member {k}")
+            ref.close()
+    finally:
+        for s in batched:
+            s.close()
