@@ -51,7 +51,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["cupic", "reference"], default="cupic")
-    ap.add_argument("--workload", choices=["large", "precision", "small", "tiny"], default="large")
+    ap.add_argument("--workload", choices=["large", "precision", "small", "tiny", "batched", "serving"],
+                    default="large")
+    ap.add_argument("--instances", type=int, default=256,
+                    help="batched: probe-bias instances (sizes drawn from seed 2)")
+    ap.add_argument("--requests", type=int, default=32, help="serving: requests in the stream")
+    ap.add_argument("--rate", type=float, default=100.0, help="serving: Poisson arrivals per second")
+    ap.add_argument("--solve-steps", type=int, default=300, help="serving: steps per request")
+    ap.add_argument("--no-plain", action="store_true", help="batched: skip the one-at-a-time run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncy", type=int, default=0,
@@ -405,11 +412,97 @@ def run_cupic(args, world, rank, local):
     return 0
 
 
+def run_batched(args, local):
+    """The batched form: probe-bias instances of uneven sizes stepped
+    together, against the same instances stepped one at a time."""
+    import cupic_gb300 as cg
+    from cupic_gb300.params import bias_instances
+    ps = bias_instances(args.instances, seed=2, sweeps=200)
+    sims = []
+    for p in ps:
+        s = cg.Sim(p, device=local)
+        s.init_plasma()
+        sims.append(s)
+    parts = float(sum(sum(s.counts()) for s in sims))
+    k = args.steps
+    # plain: each instance alone, its own graph, one after another
+    plain_s = float("nan")
+    if not args.no_plain:
+        for s in sims:
+            s.step(args.warmup)
+        t0 = time.perf_counter()
+        for s in sims:
+            s.step(k)
+        plain_s = time.perf_counter() - t0
+    b = cg.Batch(sims, device=local)
+    b.step(args.warmup)
+    sampler = ClockSampler(local)
+    sampler.start()
+    t0 = time.perf_counter()
+    b.step(k)
+    batch_s = time.perf_counter() - t0
+    clocks = sampler.stop()
+    n = len(sims)
+    line = {
+        "metric": "instance-steps/s, probe-bias instances of uneven sizes (batched form)",
+        "value": n * k / batch_s, "unit": "instance-steps/s", "n_gpus": 1, "steps": k,
+        "warmup": args.warmup, "ms_per_step": 1e3 * batch_s / k, "higher_is_better": True,
+        "particle_steps_per_s": parts * k / batch_s,
+        "plain": {"value": n * k / plain_s, "particle_steps_per_s": parts * k / plain_s,
+                  "ms_per_step_all_instances": 1e3 * plain_s / k},
+        "speedup_vs_plain": plain_s / batch_s, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{n} instances: Nx in {{32,64,128,256}}, Ny=4Nx, 10-50 particles "
+                               f"per cell per species, phi_p in [-10,2], mi/me=1836, Ti/Te=0.1, "
+                               f"200 Jacobi sweeps, seeds from 2",
+                   "particles": parts, "cells": sum(p.ncx * p.ncy for p in ps)},
+        "clocks": clocks,
+    }
+    b.close()
+    for s in sims:
+        s.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_serving(args, local):
+    """The serving loop against the plain one-at-a-time method on the same
+    Poisson request stream; every result must be identical."""
+    import copy
+    from cupic_gb300 import serve
+    from cupic_gb300.params import bias_instances
+    ps = bias_instances(args.requests, seed=3, sweeps=200)
+    t = serve.poisson_arrivals(args.requests, args.rate, seed=3)
+    reqs = [serve.Request(k, p, float(t[k]), steps=args.solve_steps,
+                          window=min(1000, args.solve_steps // 2)) for k, p in enumerate(ps)]
+    plain = serve.serve_plain(copy.deepcopy(reqs), device=local)
+    mixed = serve.serve_batched(copy.deepcopy(reqs), device=local)
+    sp, sm = serve.summary(plain), serve.summary(mixed)
+    same = all(a.current == b.current for a, b in
+               zip(sorted(plain, key=lambda r: r.rid), sorted(mixed, key=lambda r: r.rid)))
+    line = {
+        "metric": "bias-point solves/s (continuous batching)", "value": sm["solves_per_s"],
+        "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
+        "p50_ms": sm["p50_ms"], "p99_ms": sm["p99_ms"],
+        "plain": sp, "speedup_vs_plain": sm["solves_per_s"] / sp["solves_per_s"],
+        "results_identical_to_plain": same, "dtype": "f32", "data": "synthetic",
+        "config": {"requests": args.requests, "rate_per_s": args.rate,
+                   "steps_per_request": args.solve_steps, "window": reqs[0].window,
+                   "sizes": "Nx in {32,64,128,256}, Ny=4Nx, 10-50 ppc, phi_p in [-10,2]",
+                   "admission": "16 B per particle + 12 B per cell within 96 GiB"},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup()
     if args.impl == "reference":
         return run_reference(args, world, rank)
+    if args.workload == "batched":
+        return run_batched(args, local) if rank == 0 else 0
+    if args.workload == "serving":
+        return run_serving(args, local) if rank == 0 else 0
     return run_cupic(args, world, rank, local)
 
 

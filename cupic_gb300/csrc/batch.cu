@@ -43,12 +43,17 @@ struct cupic_batch {
   size_t cap_inst = 0, cap_groups = 0, cap_rows = 0, cap_nodes = 0, cap_flags = 0, cap_res = 0,
          cap_halo = 0;
   int ngroups = 0, nctas = 0, nrows = 0, nnodes = 0, max_nnx = 0, max_ncy = 0, max_inj = 0;
+  // rows of short-row instances (ncx <= kShortRow, pushed by 256-thread
+  // blocks) come first in d_rows, then the others (512-thread blocks)
+  int nrows_short = 0, max_nnx_short = 0;
   size_t nflags = 0, jsmem = 0;
   cudaGraphExec_t graph = nullptr;
   bool graph_ok = false;
 };
 
 namespace {
+
+constexpr int kShortRow = 64;  // cells per row up to which 256-thread blocks push a row
 
 #define CU(call)                                                            \
   do {                                                                      \
@@ -240,10 +245,21 @@ int build(cupic_batch *b) {
   }
   // work lists
   std::vector<int2> rows, nodes;
-  for (int i = 0; i < n; ++i) {
-    for (int s = 0; s < inst[i].ncy; ++s) rows.push_back(make_int2(i, s));
+  b->max_nnx_short = 0;
+  for (int pass = 0; pass < 2; ++pass)
+    for (int i = 0; i < n; ++i) {
+      if ((inst[i].ncx <= kShortRow) != (pass == 0)) continue;
+      for (int s = 0; s < inst[i].ncy; ++s) rows.push_back(make_int2(i, s));
+      if (pass == 0) {
+        b->nrows_short = (int)rows.size();
+        b->max_nnx_short = std::max(b->max_nnx_short, inst[i].nnx);
+      }
+    }
+  b->nrows_short = 0;
+  for (const int2 &r : rows)
+    if (inst[r.x].ncx <= kShortRow) ++b->nrows_short;
+  for (int i = 0; i < n; ++i)
     for (int j = 0; j < inst[i].nny; ++j) nodes.push_back(make_int2(i, j));
-  }
   b->nrows = (int)rows.size();
   b->nnodes = (int)nodes.size();
   if ((rc = grow(&b->d_inst, &b->cap_inst, (size_t)n)) ||
@@ -279,7 +295,9 @@ int enqueue(cupic_batch *b) {
   CU(launch_inject_draw_batch(b->d_inst, n, b->max_inj, b->side));
   CU(cudaEventRecord(b->ev_join, b->side));
   CU(launch_zero_next_rho_batch(b->d_inst, b->d_nodes, b->nnodes, st));
-  CU(launch_push_deposit_batch(b->d_inst, b->d_rows, b->nrows, b->max_nnx, st));
+  CU(launch_push_deposit_batch(b->d_inst, b->d_rows, b->nrows_short, b->max_nnx_short, 256, st));
+  CU(launch_push_deposit_batch(b->d_inst, b->d_rows + b->nrows_short, b->nrows - b->nrows_short,
+                               b->max_nnx, 512, st));
   CU(launch_arrive_batch(b->d_inst, b->d_rows, b->nrows, st));
   CU(cudaStreamWaitEvent(st, b->ev_join, 0));
   CU(launch_inject_append_batch(b->d_inst, n, b->max_ncy, st));

@@ -18,7 +18,7 @@ cudaError_t launch_inject(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_inject_draw(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_inject_append(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_finalize(const SimArgs &a, cudaStream_t st);
-size_t push_smem_bytes(int nnx);
+size_t push_smem_bytes(int nnx, int pb = 512);
 cudaError_t push_set_smem(size_t bytes);
 
 int load_blocks(int64_t n, int num_sms);
@@ -46,7 +46,7 @@ cudaError_t launch_jacobi_batch(const SimArgs *inst, const JacobiArgs *jargs, co
 cudaError_t launch_zero_next_rho_batch(const SimArgs *inst, const int2 *node_work, int n,
                                        cudaStream_t st);
 cudaError_t launch_push_deposit_batch(const SimArgs *inst, const int2 *row_work, int n, int max_nnx,
-                                      cudaStream_t st);
+                                      int threads, cudaStream_t st);
 cudaError_t launch_arrive_batch(const SimArgs *inst, const int2 *row_work, int n, cudaStream_t st);
 cudaError_t launch_inject_draw_batch(const SimArgs *inst, int n, int max_inj_cap, cudaStream_t st);
 cudaError_t launch_inject_append_batch(const SimArgs *inst, int n, int max_ncy, cudaStream_t st);

@@ -240,16 +240,13 @@ __global__ void k_leapfrog_start(SimArgs a) {
 // and every later chunk is disjoint from it.
 // ---------------------------------------------------------------------------
 namespace {
-constexpr int kPB = 512;       // threads
+constexpr int kPB = 512;       // threads (single context; batched short rows use 256)
 constexpr int kPPT = 2;        // particles per thread per chunk
 constexpr int kStages = 2;     // chunks in flight
-constexpr int kCH = kPB * kPPT;
-// scan entries per chunk: one per (particle slot j, warp), 32 particles each
-constexpr int kNE = kPPT * (kPB / 32);
-static_assert(kNE <= 32, "one warp scans a chunk's entries");
+// a chunk's scan has one entry per (particle slot j, warp), 32 particles each
 
 // three counts packed in 32 bits: 10 + 11 + 11 bits, enough for every
-// exclusive prefix of a chunk (at most 32*(kNE-1) = 992)
+// exclusive prefix of a chunk (at most 32*(32-1) = 992)
 __device__ __forceinline__ uint32_t pack3(int a, int b, int c) {
   return (uint32_t)a | ((uint32_t)b << 10) | ((uint32_t)c << 21);
 }
@@ -258,19 +255,22 @@ __device__ __forceinline__ uint32_t field1(uint32_t v) { return (v >> 10) & 0x7f
 __device__ __forceinline__ uint32_t field2(uint32_t v) { return v >> 21; }
 }  // namespace
 
-size_t push_smem_bytes(int nnx) {
-  return (size_t)kStages * kCH * sizeof(float4) + rho_moment_bytes(3, nnx - 1) +
+size_t push_smem_bytes(int nnx, int pb) {
+  return (size_t)kStages * pb * kPPT * sizeof(float4) + rho_moment_bytes(3, nnx - 1) +
          (size_t)2 * nnx * sizeof(float2);
 }
 
+template <int PB>
 __device__ __forceinline__ void push_row(const SimArgs &a, const int s, unsigned char *push_raw) {
-  constexpr int NW = kPB / 32;
-  constexpr int NE = kNE;  // scan entries per chunk, (j, warp) in j-major order
+  constexpr int NW = PB / 32;
+  constexpr int CH = PB * kPPT;                // particles per chunk
+  constexpr int NE = kPPT * NW;  // scan entries per chunk, (j, warp) in j-major order
+  static_assert(NE <= 32, "one warp scans a chunk's entries");
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nnx = a.nnx;
   const int ncx = a.ncx;
   float4 *stage = reinterpret_cast<float4 *>(push_raw);
-  float2 *etile = reinterpret_cast<float2 *>(stage + kStages * kCH);  // node rows s, s+1
+  float2 *etile = reinterpret_cast<float2 *>(stage + kStages * CH);  // node rows s, s+1
   unsigned *tmom = reinterpret_cast<unsigned *>(etile + 2 * nnx);      // cell rows s-1..s+1
   __shared__ __align__(8) uint64_t full[kStages];
   __shared__ uint32_t wsum[2][NE];  // per-entry packed counts, alternate chunks
@@ -278,7 +278,7 @@ __device__ __forceinline__ void push_row(const SimArgs &a, const int s, unsigned
 
   Ctl *ctl = a.ctl;
   const int n0 = a.sp[0].cnt[s], n1 = a.sp[1].cnt[s];
-  const int nc0 = (n0 + kCH - 1) / kCH, nct = nc0 + (n1 + kCH - 1) / kCH;
+  const int nc0 = (n0 + CH - 1) / CH, nct = nc0 + (n1 + CH - 1) / CH;
   float4 *row0 = a.sp[0].parts + a.sp[0].seg[s];
   float4 *row1 = a.sp[1].parts + a.sp[1].seg[s];
 
@@ -293,15 +293,15 @@ __device__ __forceinline__ void push_row(const SimArgs &a, const int s, unsigned
       const bool sp1 = k >= nc0;
       const int q = sp1 ? k - nc0 : k;
       const int nn = sp1 ? n1 : n0;
-      const int cnt = min(kCH, nn - q * kCH);
+      const int cnt = min(CH, nn - q * CH);
       mbar_arrive_expect_tx(&full[k], (uint32_t)cnt * 16u);
-      bulk_g2s(stage + k * kCH, (sp1 ? row1 : row0) + (size_t)q * kCH, (uint32_t)cnt * 16u, &full[k]);
+      bulk_g2s(stage + k * CH, (sp1 ? row1 : row0) + (size_t)q * CH, (uint32_t)cnt * 16u, &full[k]);
     }
   }
   RhoMoments T{tmom, s - 1, 3, ncx, nnx, a.nny, a.rho[ctl->cur ^ 1]};
   int since_fold = 0;  // chunks deposited since the last fold
   T.zero();
-  for (int k = tid; k < 2 * nnx; k += kPB) etile[k] = a.E[(size_t)s * nnx + k];
+  for (int k = tid; k < 2 * nnx; k += PB) etile[k] = a.E[(size_t)s * nnx + k];
   __syncthreads();
 
   uint32_t fl = 0;
@@ -320,15 +320,15 @@ __device__ __forceinline__ void push_row(const SimArgs &a, const int s, unsigned
     const int st = k % kStages;
     if (!mbar_wait(&full[st], (uint32_t)((k / kStages) & 1))) fl |= CUPIC_FLAG_TIMEOUT;
     const float dtqm = a.dtqm[sp];
-    const int cnt = min(kCH, nn - q * kCH);
+    const int cnt = min(CH, nn - q * CH);
     float4 p[kPPT];
     int cat[kPPT];
 #pragma unroll
     for (int j = 0; j < kPPT; ++j) {
-      const int idx = j * kPB + tid;
+      const int idx = j * PB + tid;
       cat[j] = 3;  // 0 stay, 1 up, 2 down, 3 none
       if (idx < cnt) {
-        float4 v = stage[st * kCH + idx];
+        float4 v = stage[st * CH + idx];
         float ex, ey;
         gather_tile(a, etile, v.x, v.y, s, ex, ey);
         v.z = __fmaf_rn(dtqm, ex, v.z);
@@ -364,9 +364,9 @@ __device__ __forceinline__ void push_row(const SimArgs &a, const int s, unsigned
       const bool sp1 = k2 >= nc0;
       const int q2 = sp1 ? k2 - nc0 : k2;
       const int nn2 = sp1 ? n1 : n0;
-      const int cnt2 = min(kCH, nn2 - q2 * kCH);
+      const int cnt2 = min(CH, nn2 - q2 * CH);
       mbar_arrive_expect_tx(&full[st], (uint32_t)cnt2 * 16u);
-      bulk_g2s(stage + st * kCH, (sp1 ? row1 : row0) + (size_t)q2 * kCH, (uint32_t)cnt2 * 16u,
+      bulk_g2s(stage + st * CH, (sp1 ? row1 : row0) + (size_t)q2 * CH, (uint32_t)cnt2 * 16u,
                &full[st]);
     }
     // Every warp scans the chunk's NE entries itself (no second barrier).
@@ -411,7 +411,7 @@ __device__ __forceinline__ void push_row(const SimArgs &a, const int s, unsigned
     // fold at the end of a species and before the moments could overflow
     // (block-uniform); the next deposits follow the next chunk's barrier
     ++since_fold;
-    if (k + 1 < nct && (k + 1 == nc0 || (since_fold + 1) * kCH > kFoldParticles)) {
+    if (k + 1 < nct && (k + 1 == nc0 || (since_fold + 1) * CH > kFoldParticles)) {
       __syncthreads();
       T.fold(qc);
       since_fold = 0;
@@ -444,15 +444,25 @@ __device__ __forceinline__ void push_row(const SimArgs &a, const int s, unsigned
 
 __global__ void __launch_bounds__(kPB, 3) k_push_deposit(SimArgs a) {
   extern __shared__ __align__(128) unsigned char push_raw[];
-  push_row(a, blockIdx.x, push_raw);
+  push_row<kPB>(a, blockIdx.x, push_raw);
 }
 
-// many contexts in one launch: work[b] = {instance, row}
-__global__ void __launch_bounds__(kPB, 3)
+// many contexts in one launch: work[b] = {instance, row}; PB = 256 for
+// short rows (more blocks per SM), 512 otherwise
+template <int PB>
+__global__ void __launch_bounds__(PB, PB == 256 ? 4 : 2)
     k_push_deposit_batch(const SimArgs *__restrict__ inst, const int2 *__restrict__ work) {
   extern __shared__ __align__(128) unsigned char push_raw[];
+  // the instance's arguments in shared memory: read there as needed instead
+  // of held in registers
+  __shared__ __align__(16) SimArgs sa;
   const int2 w = work[blockIdx.x];
-  push_row(inst[w.x], w.y, push_raw);
+  static_assert(sizeof(SimArgs) % 4 == 0, "");
+  const unsigned *src = reinterpret_cast<const unsigned *>(inst + w.x);
+  unsigned *dst = reinterpret_cast<unsigned *>(&sa);
+  for (int k = threadIdx.x; k < (int)(sizeof(SimArgs) / 4); k += PB) dst[k] = src[k];
+  __syncthreads();
+  push_row<PB>(sa, w.y, push_raw);
 }
 
 // ---------------------------------------------------------------------------
@@ -739,7 +749,7 @@ cudaError_t push_set_smem(size_t bytes) {
 }
 
 cudaError_t launch_push_deposit(const SimArgs &a, cudaStream_t st) {
-  const size_t sm = push_smem_bytes(a.nnx);
+  const size_t sm = push_smem_bytes(a.nnx, kPB);
   k_push_deposit<<<a.ncy, kPB, sm, st>>>(a);
   return cudaGetLastError();
 }
@@ -777,18 +787,25 @@ cudaError_t launch_zero_next_rho_batch(const SimArgs *inst, const int2 *node_wor
   return cudaGetLastError();
 }
 
-cudaError_t launch_push_deposit_batch(const SimArgs *inst, const int2 *row_work, int n, int max_nnx,
-                                      cudaStream_t st) {
+template <int PB>
+cudaError_t push_batch(const SimArgs *inst, const int2 *row_work, int n, int max_nnx, cudaStream_t st) {
   static size_t cur = 48 * 1024;  // the attribute only grows
-  const size_t sm = push_smem_bytes(max_nnx);
+  const size_t sm = push_smem_bytes(max_nnx, PB);
   if (sm > cur) {
-    cudaError_t e = cudaFuncSetAttribute(k_push_deposit_batch,
+    cudaError_t e = cudaFuncSetAttribute(k_push_deposit_batch<PB>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
     cur = sm;
   }
-  k_push_deposit_batch<<<n, kPB, sm, st>>>(inst, row_work);
+  k_push_deposit_batch<PB><<<n, PB, sm, st>>>(inst, row_work);
   return cudaGetLastError();
+}
+
+cudaError_t launch_push_deposit_batch(const SimArgs *inst, const int2 *row_work, int n, int max_nnx,
+                                      int threads, cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  return threads == 256 ? push_batch<256>(inst, row_work, n, max_nnx, st)
+                        : push_batch<512>(inst, row_work, n, max_nnx, st);
 }
 
 cudaError_t launch_arrive_batch(const SimArgs *inst, const int2 *row_work, int n, cudaStream_t st) {

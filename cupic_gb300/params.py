@@ -125,3 +125,32 @@ def workload_params(name="small", **over):
     for k, v in over.items():
         setattr(p, k, v)
     return p.finalize()
+
+
+def bias_instances(n=256, seed=2, sweeps=200, sizes=(32, 64, 128, 256)):
+    """Probe-bias instances of uneven sizes, drawn from `seed`: Nx uniform in
+    `sizes`, Ny = 4 Nx, ds = 0.5, particles per cell per species uniform in
+    10..50, phi_p uniform in [-10, 2], mi/me = 1836, Ti/Te = 0.1,
+    dt = 0.05, `sweeps` Jacobi sweeps per step.  Instance i has its own
+    generator seed."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        nx = int(rng.choice(sizes))
+        ppc = int(rng.integers(10, 51))
+        phi_p = float(rng.uniform(-10.0, 2.0))
+        p = workload_params("large", ncx=nx, ncy=4 * nx, phi_p=phi_p, seed=seed * 100000 + i,
+                            min_sweeps=sweeps, max_sweeps=sweeps, check_every=sweeps,
+                            init_min_sweeps=sweeps, init_max_sweeps=sweeps)
+        p.n = ppc / p.ds ** 3
+        p.eps0 = p.n
+        out.append(p.finalize())
+    return out
+
+
+def footprint_bytes(p):
+    """Admission footprint of an instance: 16 B per particle of both
+    species plus 12 B per cell."""
+    cells = p.ncx * p.ncy
+    return 16 * 2 * p.ppr * p.ncy + 12 * cells

@@ -1,0 +1,151 @@
+"""Serving loop for bias-point requests, and the plain one-at-a-time loop it
+is measured against.  There is no counterpart in the reference, which runs
+one simulation per process.
+
+A request is one probe-bias instance (a Params set) to run for `steps`
+steps; its result is the time-averaged probe current over the last `window`
+steps: the net charge absorbed by the probe per step, ions minus electrons.
+
+Continuous batching (``serve_batched``): requests that have arrived are
+admitted while their footprint (16 B per particle plus 12 B per cell) fits
+the HBM budget and a slot is free; their state is created and initialised
+on the device while the running members step, and they join the batch at
+the next tick.  A tick is one ``Batch.step`` of all members (at most `tick`
+steps, never past a member's last step); members that finish leave the
+batch and free their footprint.  A member's result is bit-identical to the
+one it gets alone, because batched and solo steps compute the same thing.
+"""
+import collections
+import dataclasses
+import time
+
+import numpy as np
+
+from . import Batch, Sim
+from .params import footprint_bytes
+
+
+@dataclasses.dataclass
+class Request:
+    rid: int
+    params: object
+    arrival: float          # seconds after the start of the run
+    steps: int = 2000
+    window: int = 1000
+    start: float = None     # admission time
+    finish: float = None    # result time
+    current: float = None   # mean net absorbed charge per step over the window
+
+    @property
+    def latency(self):
+        return self.finish - self.arrival
+
+
+def poisson_arrivals(n, rate, seed=3):
+    """Arrival times of n requests of a Poisson stream of `rate` per second."""
+    rng = np.random.default_rng(seed)
+    return np.cumsum(rng.exponential(1.0 / rate, size=n))
+
+
+def probe_current(sim, window):
+    st = sim.stats(window)
+    return float(np.mean([s["absorbed"][1] - s["absorbed"][0] for s in st]))
+
+
+def warm_plans(requests, device=0):
+    """Creates one context per distinct mesh shape so that the solver layout
+    of each shape is tuned (and cached) before the clock starts."""
+    seen = set()
+    for r in requests:
+        p = r.params
+        key = (p.ncx, p.ncy, p.check_every, p.max_sweeps, p.init_max_sweeps)
+        if key not in seen:
+            seen.add(key)
+            Sim(p, device=device).close()
+
+
+def serve_batched(requests, budget_bytes=96 << 30, max_slots=512, tick=50, device=0,
+                  clock=time.perf_counter):
+    """Runs the requests with continuous batching in real time; fills in
+    start, finish and current of every request and returns them."""
+    warm_plans(requests, device)
+    pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
+    queue = collections.deque()
+    active = []   # [request, sim, steps done]
+    joining = []
+    used = 0
+    batch = Batch(device=device)
+    t0 = clock()
+    try:
+        while pending or queue or active or joining:
+            stepping = bool(active)
+            k = 0
+            if stepping:
+                k = min(tick, min(r.steps - d for r, _, d in active))
+                batch.step(k, sync=False)
+            now = clock() - t0
+            while pending and pending[0].arrival <= now:
+                queue.append(pending.popleft())
+            while queue and len(active) + len(joining) < max_slots:
+                fp = footprint_bytes(queue[0].params)
+                if used + fp > budget_bytes:
+                    if not active and not joining:
+                        raise RuntimeError(f"request {queue[0].rid} exceeds the HBM budget")
+                    break
+                r = queue.popleft()
+                sim = Sim(r.params, device=device)
+                sim.init_plasma()
+                r.start = clock() - t0
+                joining.append([r, sim, 0])
+                used += fp
+            if stepping:
+                batch.sync()
+                for a in active:
+                    a[2] += k
+            done = [a for a in active if a[2] >= a[0].steps]
+            for r, sim, _ in done:
+                r.current = probe_current(sim, r.window)
+                r.finish = clock() - t0
+            if done or joining:
+                active = [a for a in active if a[2] < a[0].steps] + joining
+                joining = []
+                batch.set([a[1] for a in active])
+            for r, sim, _ in done:
+                sim.close()
+                used -= footprint_bytes(r.params)
+            if not active and not queue and pending:
+                time.sleep(max(0.0, pending[0].arrival - (clock() - t0)))
+    finally:
+        batch.close()
+        for a in active + joining:
+            a[1].close()
+    return requests
+
+
+def serve_plain(requests, device=0, clock=time.perf_counter):
+    """The plain method: one request at a time in arrival order, each stepped
+    alone (cupic_step), in real time."""
+    warm_plans(requests, device)
+    t0 = clock()
+    for r in sorted(requests, key=lambda q: q.arrival):
+        wait = r.arrival - (clock() - t0)
+        if wait > 0:
+            time.sleep(wait)
+        r.start = clock() - t0
+        sim = Sim(r.params, device=device)
+        try:
+            sim.init_plasma()
+            sim.step(r.steps)
+            r.current = probe_current(sim, r.window)
+        finally:
+            sim.close()
+        r.finish = clock() - t0
+    return requests
+
+
+def summary(requests):
+    lat = np.array([r.latency for r in requests])
+    span = max(r.finish for r in requests) - min(r.arrival for r in requests)
+    return {"solves": len(requests), "seconds": span, "solves_per_s": len(requests) / span,
+            "p50_ms": 1e3 * float(np.percentile(lat, 50)),
+            "p99_ms": 1e3 * float(np.percentile(lat, 99))}
