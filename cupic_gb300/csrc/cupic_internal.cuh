@@ -270,10 +270,13 @@ __device__ __forceinline__ void gather_tile4(const SimArgs &a, const float4 *til
   Epy = ey;
 }
 
-// fixed-point CIC weights (16 fractional bits per axis, 2^32 per particle)
+// fixed-point CIC weights: 16 fractional bits per axis and the cross term
+// FX*FY rounded to a multiple of 2^16, so the four weights are exact
+// integers that sum to 2^32 per particle
 struct CicFixed {
   int ic, jc;
   int FX, FY;  // offsets in the cell, 16 fractional bits, in [0, 65536]
+  int FXY;     // round(FX*FY / 2^16), in [0, 65536]
   long long w00, w10, w01, w11;
 };
 
@@ -287,12 +290,12 @@ __device__ __forceinline__ CicFixed cic_fixed(const SimArgs &a, float x, float y
   const float fy = clamp01f(__fsub_rn(sy, (float)r.jc));
   r.FX = __float2int_rn(__fmul_rn(fx, 65536.0f));
   r.FY = __float2int_rn(__fmul_rn(fy, 65536.0f));
-  const long long FX = r.FX, FY = r.FY;
-  const long long GX = 65536 - FX, GY = 65536 - FY;
-  r.w00 = GX * GY;
-  r.w10 = FX * GY;
-  r.w01 = GX * FY;
-  r.w11 = FX * FY;
+  r.FXY = (int)(((unsigned long long)r.FX * (unsigned long long)r.FY + 32768ull) >> 16);
+  const long long FX = r.FX, FY = r.FY, W11 = (long long)r.FXY << 16;
+  r.w11 = W11;
+  r.w10 = (FX << 16) - W11;
+  r.w01 = (FY << 16) - W11;
+  r.w00 = 4294967296ll - ((FX + FY) << 16) + W11;
   return r;
 }
 

@@ -28,27 +28,28 @@ __device__ __forceinline__ void raise_flags(Ctl *ctl, uint32_t f) {
   if (f) atomicOr(&ctl->step_flags, f);
 }
 
-// Charge deposition into shared memory by cell moments.  For the particles
-// of a cell, with 16-bit fixed-point offsets FX, FY in [0, 65536] and
-// GX = 65536-FX, GY = 65536-FY, the four node sums of the weights follow
-// exactly from four integer moments of the cell:
-//   sum GX GY = 65536^2 M1 - 65536 (MX + MY) + MXY      (lower-left node)
-//   sum FX GY = 65536 MX - MXY                          (lower-right)
-//   sum GX FY = 65536 MY - MXY                          (upper-left)
-//   sum FX FY = MXY                                     (upper-right)
-// with M1 = count, MX = sum FX, MY = sum FY, MXY = sum FX FY.  Shared memory
-// atomics are native for 32-bit integers only, so a particle adds 1, FX, FY
-// and the two 16-bit halves of FX FY to the five unsigned moments of its
-// cell (stored together, one address per particle).  The moments of one
-// species over at most kFoldParticles particles stay below 2^32; fold(q)
-// turns them into int64 node sums times the species charge q, added to
-// global memory, that often and at every change of species.  Deposits whose
-// cell row is outside the tile go straight to global memory as int64 node
-// weights.
+// Charge deposition into shared memory by cell moments.  A particle with
+// 16-bit fixed-point offsets FX, FY in [0, 65536] in its cell and cross term
+// FXY = round(FX*FY / 2^16) (cic_fixed) gives its four nodes the weights
+//   upper-right w11 = 2^16 FXY,          lower-right w10 = 2^16 FX - w11,
+//   upper-left  w01 = 2^16 FY - w11,     lower-left  w00 = 2^32 - 2^16 (FX + FY) + w11,
+// the CIC weights with FX*FY rounded to a multiple of 2^16; they sum to 2^32.
+// Over the particles of a cell the four node sums follow from four integer
+// moments M1 = count, MX = sum FX, MY = sum FY, MXY = sum FXY by the same
+// formulas.  Shared memory atomics are native for 32-bit integers only, so
+// a particle adds 1, FX, FY and FXY to the four unsigned moments of its cell
+// (stored together at an odd stride, one address per particle).  The moments of one species
+// over at most kFoldParticles particles stay below 2^32; fold(q) turns them
+// into int64 node sums times the species charge q, added to global memory,
+// that often and at every change of species.  Deposits whose cell row is
+// outside the tile go straight to global memory as int64 node weights.
 constexpr int kFoldParticles = 63 * 1024;  // 64512 * 65536 < 2^32
+// words per cell: odd, so that lanes depositing to different cells of a
+// row hit different shared-memory banks
+constexpr int kMomStride = 5;
 
 struct RhoMoments {
-  unsigned *m;     // [ncr*ncx][5]: M1, MX, MY, MXY >> 16, MXY & 0xffff
+  unsigned *m;     // [ncr*ncx][kMomStride]: M1, MX, MY, MXY (and one unused word)
   int crow0, ncr, ncx, nnx, nny;
   unsigned long long *g;
 
@@ -56,13 +57,11 @@ struct RhoMoments {
     const CicFixed c = cic_fixed(a, x, y);
     const int tr = c.jc - crow0;
     if (tr >= 0 && tr < ncr) {
-      unsigned *mc = m + 5 * (tr * ncx + c.ic);
-      const unsigned long long fxy = (unsigned long long)c.FX * (unsigned long long)c.FY;
+      unsigned *mc = m + kMomStride * (tr * ncx + c.ic);
       atomicAdd(mc, 1u);
       atomicAdd(mc + 1, (unsigned)c.FX);
       atomicAdd(mc + 2, (unsigned)c.FY);
-      atomicAdd(mc + 3, (unsigned)(fxy >> 16));
-      atomicAdd(mc + 4, (unsigned)(fxy & 0xffffull));
+      atomicAdd(mc + 3, (unsigned)c.FXY);
     } else {
       const size_t n00 = (size_t)c.jc * nnx + c.ic;
       atomicAdd(&g[n00], (unsigned long long)(q * c.w00));
@@ -72,10 +71,10 @@ struct RhoMoments {
     }
   }
   __device__ __forceinline__ void zero() const {
-    for (int k = threadIdx.x; k < 5 * ncr * ncx; k += blockDim.x) m[k] = 0u;
+    for (int k = threadIdx.x; k < kMomStride * ncr * ncx; k += blockDim.x) m[k] = 0u;
   }
   __device__ __forceinline__ long long mxy(int c) const {
-    return (long long)m[5 * c + 3] * 65536 + (long long)m[5 * c + 4];
+    return (long long)m[kMomStride * c + 3] << 16;
   }
   // moments (of charge q particles) -> node sums added to global memory,
   // then clear the moments; callers __syncthreads() before, and before the
@@ -86,16 +85,16 @@ struct RhoMoments {
       long long v = 0;
       if (i < ncx && j < ncr) {  // this node is the lower-left corner of cell (i, j)
         const int c = j * ncx + i;
-        v += (long long)m[5 * c] * 4294967296ll -
-             65536ll * ((long long)m[5 * c + 1] + (long long)m[5 * c + 2]) + mxy(c);
+        v += (long long)m[kMomStride * c] * 4294967296ll -
+             65536ll * ((long long)m[kMomStride * c + 1] + (long long)m[kMomStride * c + 2]) + mxy(c);
       }
       if (i >= 1 && j < ncr) {  // lower-right corner of cell (i-1, j)
         const int c = j * ncx + i - 1;
-        v += 65536ll * (long long)m[5 * c + 1] - mxy(c);
+        v += 65536ll * (long long)m[kMomStride * c + 1] - mxy(c);
       }
       if (i < ncx && j >= 1) {  // upper-left corner of cell (i, j-1)
         const int c = (j - 1) * ncx + i;
-        v += 65536ll * (long long)m[5 * c + 2] - mxy(c);
+        v += 65536ll * (long long)m[kMomStride * c + 2] - mxy(c);
       }
       if (i >= 1 && j >= 1) {  // upper-right corner of cell (i-1, j-1)
         v += mxy((j - 1) * ncx + i - 1);
@@ -105,7 +104,7 @@ struct RhoMoments {
         atomicAdd(&g[(size_t)r * nnx + i], (unsigned long long)(q * v));
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < 5 * ncr * ncx; k += blockDim.x) m[k] = 0u;
+    for (int k = threadIdx.x; k < kMomStride * ncr * ncx; k += blockDim.x) m[k] = 0u;
   }
 };
 

@@ -269,14 +269,16 @@ struct Sim {
     const R fy = clamp01<R>(sy - (R)jc);
     const size_t n00 = (size_t)jc * nnx + ic;
     if constexpr (F32) {
+      /* CIC weights in 16-bit fixed point per axis, the cross term FX*FY
+       * rounded to a multiple of 2^16; the four sum to 2^32 */
       const int64_t FX = (int64_t)std::rint(fx * 65536.0f);
       const int64_t FY = (int64_t)std::rint(fy * 65536.0f);
-      const int64_t GX = 65536 - FX, GY = 65536 - FY;
+      const int64_t W11 = ((FX * FY + 32768) >> 16) << 16;
       const int64_t qq = qs < 0 ? -1 : 1;
-      sink(n00, qq * GX * GY);
-      sink(n00 + 1, qq * FX * GY);
-      sink(n00 + nnx, qq * GX * FY);
-      sink(n00 + nnx + 1, qq * FX * FY);
+      sink(n00, qq * ((int64_t)1 << 32) - qq * ((FX + FY) << 16) + qq * W11);
+      sink(n00 + 1, qq * ((FX << 16) - W11));
+      sink(n00 + nnx, qq * ((FY << 16) - W11));
+      sink(n00 + nnx + 1, qq * W11);
     } else {
       const double gx = 1.0 - fx, gy = 1.0 - fy;
       sink(n00, qs * gx * gy);
