@@ -9,6 +9,8 @@
 //     fewest CTAs that hold them), groups sized and filled by the members'
 //     mesh work (largest first onto the least-loaded group);
 //   - push, arrive and the charge clear: work lists of {instance, row};
+//     instances of 512 rows or more, which fill the GPU by themselves, are
+//     pushed by the single-context kernel on parallel graph branches;
 //   - the injection draws (beside the push, on a side stream), the append
 //     and the bookkeeping: one block or thread per instance and species.
 // Every kernel reads its instance's SimArgs from a device array, so members
@@ -43,9 +45,14 @@ struct cupic_batch {
   size_t cap_inst = 0, cap_groups = 0, cap_rows = 0, cap_nodes = 0, cap_flags = 0, cap_res = 0,
          cap_halo = 0;
   int ngroups = 0, nctas = 0, nrows = 0, nnodes = 0, max_nnx = 0, max_ncy = 0, max_inj = 0;
-  // rows of short-row instances (ncx <= kShortRow, pushed by 256-thread
-  // blocks) come first in d_rows, then the others (512-thread blocks)
-  int nrows_short = 0, max_nnx_short = 0;
+  // d_rows: rows of short-row instances (ncx <= kShortRow, pushed by
+  // 256-thread blocks), then rows of mid-size ones (512-thread blocks),
+  // then rows of big ones (ncy >= kBigRows), which are pushed by the
+  // single-context kernel, one launch per instance on parallel branches
+  int nrows_short = 0, nrows_mid = 0, max_nnx_short = 0, max_nnx_mid = 0;
+  std::vector<int> big;  // member indices pushed one launch each
+  cudaStream_t push_st[4] = {};
+  cudaEvent_t ev_push_fork = nullptr, ev_push_join[4] = {};
   size_t nflags = 0, jsmem = 0;
   cudaGraphExec_t graph = nullptr;
   bool graph_ok = false;
@@ -54,6 +61,8 @@ struct cupic_batch {
 namespace {
 
 constexpr int kShortRow = 64;  // cells per row up to which 256-thread blocks push a row
+constexpr int kBigRows = 512;  // rows from which an instance fills the GPU by itself
+constexpr int kPushBranches = 4;
 
 #define CU(call)                                                            \
   do {                                                                      \
@@ -245,19 +254,22 @@ int build(cupic_batch *b) {
   }
   // work lists
   std::vector<int2> rows, nodes;
-  b->max_nnx_short = 0;
-  for (int pass = 0; pass < 2; ++pass)
+  b->max_nnx_short = b->max_nnx_mid = 0;
+  b->big.clear();
+  auto cls = [&](int i) { return inst[i].ncy >= kBigRows ? 2 : inst[i].ncx <= kShortRow ? 0 : 1; };
+  for (int pass = 0; pass < 3; ++pass)
     for (int i = 0; i < n; ++i) {
-      if ((inst[i].ncx <= kShortRow) != (pass == 0)) continue;
+      if (cls(i) != pass) continue;
       for (int s = 0; s < inst[i].ncy; ++s) rows.push_back(make_int2(i, s));
-      if (pass == 0) {
-        b->nrows_short = (int)rows.size();
-        b->max_nnx_short = std::max(b->max_nnx_short, inst[i].nnx);
-      }
+      if (pass == 0) b->max_nnx_short = std::max(b->max_nnx_short, inst[i].nnx);
+      if (pass == 1) b->max_nnx_mid = std::max(b->max_nnx_mid, inst[i].nnx);
+      if (pass == 2) b->big.push_back(i);
     }
-  b->nrows_short = 0;
-  for (const int2 &r : rows)
-    if (inst[r.x].ncx <= kShortRow) ++b->nrows_short;
+  b->nrows_short = b->nrows_mid = 0;
+  for (const int2 &r : rows) {
+    if (cls(r.x) == 0) ++b->nrows_short;
+    if (cls(r.x) == 1) ++b->nrows_mid;
+  }
   for (int i = 0; i < n; ++i)
     for (int j = 0; j < inst[i].nny; ++j) nodes.push_back(make_int2(i, j));
   b->nrows = (int)rows.size();
@@ -295,9 +307,20 @@ int enqueue(cupic_batch *b) {
   CU(launch_inject_draw_batch(b->d_inst, n, b->max_inj, b->side));
   CU(cudaEventRecord(b->ev_join, b->side));
   CU(launch_zero_next_rho_batch(b->d_inst, b->d_nodes, b->nnodes, st));
+  // big instances: the single-context push, one launch each, on parallel
+  // branches beside the work-list pushes of the others
+  const int nbr = b->big.empty() ? 0 : std::min(kPushBranches, (int)b->big.size());
+  if (nbr) {
+    CU(cudaEventRecord(b->ev_push_fork, st));
+    for (int k = 0; k < nbr; ++k) CU(cudaStreamWaitEvent(b->push_st[k], b->ev_push_fork, 0));
+    for (size_t q = 0; q < b->big.size(); ++q)
+      CU(launch_push_deposit(b->members[b->big[q]]->a, b->push_st[q % nbr]));
+    for (int k = 0; k < nbr; ++k) CU(cudaEventRecord(b->ev_push_join[k], b->push_st[k]));
+  }
   CU(launch_push_deposit_batch(b->d_inst, b->d_rows, b->nrows_short, b->max_nnx_short, 256, st));
-  CU(launch_push_deposit_batch(b->d_inst, b->d_rows + b->nrows_short, b->nrows - b->nrows_short,
-                               b->max_nnx, 512, st));
+  CU(launch_push_deposit_batch(b->d_inst, b->d_rows + b->nrows_short, b->nrows_mid, b->max_nnx_mid,
+                               512, st));
+  for (int k = 0; k < nbr; ++k) CU(cudaStreamWaitEvent(st, b->ev_push_join[k], 0));
   CU(launch_arrive_batch(b->d_inst, b->d_rows, b->nrows, st));
   CU(cudaStreamWaitEvent(st, b->ev_join, 0));
   CU(launch_inject_append_batch(b->d_inst, n, b->max_ncy, st));
@@ -342,10 +365,17 @@ int cupic_batch_create(int device, cupic_batch **out) {
       cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+      cudaEventCreateWithFlags(&b->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&b->ev_push_fork, cudaEventDisableTiming) != cudaSuccess) {
     cupic_batch_destroy(b);
     return CUPIC_ERR_CUDA;
   }
+  for (int k = 0; k < kPushBranches; ++k)
+    if (cudaStreamCreateWithFlags(&b->push_st[k], cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->ev_push_join[k], cudaEventDisableTiming) != cudaSuccess) {
+      cupic_batch_destroy(b);
+      return CUPIC_ERR_CUDA;
+    }
   *out = b;
   return CUPIC_OK;
 }
@@ -414,6 +444,14 @@ int cupic_batch_destroy(cupic_batch *b) {
   cudaFree(b->d_res);
   cudaFree(b->d_halo);
   if (b->ev_fork) cudaEventDestroy(b->ev_fork);
+  if (b->ev_push_fork) cudaEventDestroy(b->ev_push_fork);
+  for (int k = 0; k < kPushBranches; ++k) {
+    if (b->ev_push_join[k]) cudaEventDestroy(b->ev_push_join[k]);
+    if (b->push_st[k]) {
+      cudaStreamSynchronize(b->push_st[k]);
+      cudaStreamDestroy(b->push_st[k]);
+    }
+  }
   if (b->ev_join) cudaEventDestroy(b->ev_join);
   if (b->side) {
     cudaStreamSynchronize(b->side);
