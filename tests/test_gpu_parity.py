@@ -167,3 +167,29 @@ def test_runs_are_deterministic(make_pair):
     for sp in (0, 1):
         np.testing.assert_array_equal(a.particles(sp), b.particles(sp))
     np.testing.assert_array_equal(a.rho_fixed(0), b.rho_fixed(0))
+
+
+def test_small_workload_matches_committed_golden(gpu_lib):
+    """The 64x256 workload on the GPU gives, bit for bit, the committed
+    digests of the FP32 oracle (tests/golden/oracle_small.json)."""
+    import json
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, os.path.join(root, "tests", "golden"))
+    import make_oracle_golden as mk
+    with open(os.path.join(root, "tests", "golden", "oracle_small.json")) as f:
+        gold = json.load(f)
+    with cg.Sim(cg.workload_params("small")) as sim:
+        sim.init_plasma()
+
+        def snap():
+            ex, ey = sim.efield()
+            return mk.snapshot(sim.particles, sim.row_counts, lambda: sim.rho_fixed(0), sim.phi, ex, ey)
+
+        assert snap() == gold["states"]["init"]
+        for k in range(1, 11):
+            sim.step(1)
+            st = sim.stats(1)[0]
+            assert {key: st[key] for key in gold["stats"][k - 1]} == gold["stats"][k - 1], k
+            if k in (1, 10):
+                assert snap() == gold["states"][f"step{k}"], k
