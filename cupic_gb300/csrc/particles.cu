@@ -260,9 +260,10 @@ size_t push_smem_bytes(int nnx, int pb) {
 }
 
 template <int PB>
-__device__ __forceinline__ void push_row(const SimArgs &a, const int s, unsigned char *push_raw) {
+__device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const int sp,
+                                          unsigned char *push_raw) {
   constexpr int NW = PB / 32;
-  constexpr int CH = PB * kPPT;                // particles per chunk
+  constexpr int CH = PB * kPPT;  // particles per chunk
   constexpr int NE = kPPT * NW;  // scan entries per chunk, (j, warp) in j-major order
   static_assert(NE <= 32, "one warp scans a chunk's entries");
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -273,28 +274,25 @@ __device__ __forceinline__ void push_row(const SimArgs &a, const int s, unsigned
   unsigned *tmom = reinterpret_cast<unsigned *>(etile + 2 * nnx);      // cell rows s-1..s+1
   __shared__ __align__(8) uint64_t full[kStages];
   __shared__ uint32_t wsum[2][NE];  // per-entry packed counts, alternate chunks
-  __shared__ unsigned long long s_cnt[4];
+  __shared__ unsigned long long s_cnt[2];
 
   Ctl *ctl = a.ctl;
-  const int n0 = a.sp[0].cnt[s], n1 = a.sp[1].cnt[s];
-  const int nc0 = (n0 + CH - 1) / CH, nct = nc0 + (n1 + CH - 1) / CH;
-  float4 *row0 = a.sp[0].parts + a.sp[0].seg[s];
-  float4 *row1 = a.sp[1].parts + a.sp[1].seg[s];
+  const SpeciesDev &S = a.sp[sp];
+  const int nn = S.cnt[s];
+  const int nch = (nn + CH - 1) / CH;
+  float4 *row = S.parts + S.seg[s];
 
   if (tid == 0) {
     for (int i = 0; i < kStages; ++i) mbar_init(&full[i], 1);
     fence_mbar_init();
-    for (int i = 0; i < 4; ++i) s_cnt[i] = 0ull;
+    s_cnt[0] = s_cnt[1] = 0ull;
   }
   __syncthreads();
   if (tid == 0) {
-    for (int k = 0; k < kStages && k < nct; ++k) {
-      const bool sp1 = k >= nc0;
-      const int q = sp1 ? k - nc0 : k;
-      const int nn = sp1 ? n1 : n0;
-      const int cnt = min(CH, nn - q * CH);
+    for (int k = 0; k < kStages && k < nch; ++k) {
+      const int cnt = min(CH, nn - k * CH);
       mbar_arrive_expect_tx(&full[k], (uint32_t)cnt * 16u);
-      bulk_g2s(stage + k * CH, (sp1 ? row1 : row0) + (size_t)q * CH, (uint32_t)cnt * 16u, &full[k]);
+      bulk_g2s(stage + k * CH, row + (size_t)k * CH, (uint32_t)cnt * 16u, &full[k]);
     }
   }
   RhoMoments T{tmom, s - 1, 3, ncx, nnx, a.nny, a.rho[ctl->cur ^ 1]};
@@ -304,22 +302,17 @@ __device__ __forceinline__ void push_row(const SimArgs &a, const int s, unsigned
   __syncthreads();
 
   uint32_t fl = 0;
-  unsigned nabs[2] = {0u, 0u}, nrem[2] = {0u, 0u};
+  unsigned nabs = 0u, nrem = 0u;
   const uint32_t lt = (1u << lane) - 1u;
+  const float dtqm = a.dtqm[sp];
+  const int qc = sp == 0 ? -1 : 1;
+  float4 *sup = S.stage_up + (size_t)s * S.stage_cap;
+  float4 *sdn = S.stage_down + (size_t)s * S.stage_cap;
   int c_stay = 0, c_up = 0, c_dn = 0;
-  for (int k = 0; k < nct; ++k) {
-    const int sp = k >= nc0 ? 1 : 0;
-    const int q = sp ? k - nc0 : k;
-    const int nn = sp ? n1 : n0;
-    const SpeciesDev &S = a.sp[sp];
-    float4 *row = sp ? row1 : row0;
-    if (k == nc0) {  // species boundary
-      c_stay = c_up = c_dn = 0;
-    }
+  for (int k = 0; k < nch; ++k) {
     const int st = k % kStages;
     if (!mbar_wait(&full[st], (uint32_t)((k / kStages) & 1))) fl |= CUPIC_FLAG_TIMEOUT;
-    const float dtqm = a.dtqm[sp];
-    const int cnt = min(CH, nn - q * CH);
+    const int cnt = min(CH, nn - k * CH);
     float4 p[kPPT];
     int cat[kPPT];
 #pragma unroll
@@ -338,9 +331,9 @@ __device__ __forceinline__ void push_row(const SimArgs &a, const int s, unsigned
         const Cls c = classify(a, v, s);
         fl |= c.flag;
         if (c.dest == kRowAbsorbed) {
-          ++nabs[sp];
+          ++nabs;
         } else if (c.dest == kRowRemoved) {
-          ++nrem[sp];
+          ++nrem;
         } else {
           cat[j] = c.dest == s ? 0 : (c.dest == s + 1 ? 1 : 2);
         }
@@ -358,15 +351,11 @@ __device__ __forceinline__ void push_row(const SimArgs &a, const int s, unsigned
     }
     __syncthreads();  // the only block barrier of a chunk
     // every thread holds its particles: refill this stage with chunk k+kStages
-    if (tid == 0 && k + kStages < nct) {
+    if (tid == 0 && k + kStages < nch) {
       const int k2 = k + kStages;
-      const bool sp1 = k2 >= nc0;
-      const int q2 = sp1 ? k2 - nc0 : k2;
-      const int nn2 = sp1 ? n1 : n0;
-      const int cnt2 = min(CH, nn2 - q2 * CH);
+      const int cnt2 = min(CH, nn - k2 * CH);
       mbar_arrive_expect_tx(&full[st], (uint32_t)cnt2 * 16u);
-      bulk_g2s(stage + st * CH, (sp1 ? row1 : row0) + (size_t)q2 * CH, (uint32_t)cnt2 * 16u,
-               &full[st]);
+      bulk_g2s(stage + st * CH, row + (size_t)k2 * CH, (uint32_t)cnt2 * 16u, &full[st]);
     }
     // Every warp scans the chunk's NE entries itself (no second barrier).
     // Exclusive prefixes are at most 32*(NE-1) < 1024 per field, so the
@@ -381,9 +370,6 @@ __device__ __forceinline__ void push_row(const SimArgs &a, const int s, unsigned
     }
     const uint32_t ex = inc - v;
     const uint32_t exl = __shfl_sync(kFull, ex, NE - 1), vl = __shfl_sync(kFull, v, NE - 1);
-    float4 *sup = S.stage_up + (size_t)s * S.stage_cap;
-    float4 *sdn = S.stage_down + (size_t)s * S.stage_cap;
-    const int qc = sp == 0 ? -1 : 1;
 #pragma unroll
     for (int j = 0; j < kPPT; ++j) {
       const uint32_t off = __shfl_sync(kFull, ex, j * NW + warp);
@@ -401,53 +387,46 @@ __device__ __forceinline__ void push_row(const SimArgs &a, const int s, unsigned
     c_stay += (int)(field0(exl) + field0(vl));
     c_up += (int)(field1(exl) + field1(vl));
     c_dn += (int)(field2(exl) + field2(vl));
-    const bool last_of_species = (k == nct - 1) || (k == nc0 - 1);
-    if (tid == 0 && last_of_species) {
-      S.nstay[s] = c_stay;
-      S.nup[s] = min(c_up, S.stage_cap);
-      S.ndown[s] = min(c_dn, S.stage_cap);
-    }
-    // fold at the end of a species and before the moments could overflow
-    // (block-uniform); the next deposits follow the next chunk's barrier
+    // fold before the moments could overflow (block-uniform); the next
+    // deposits follow the next chunk's barrier
     ++since_fold;
-    if (k + 1 < nct && (k + 1 == nc0 || (since_fold + 1) * CH > kFoldParticles)) {
+    if (k + 1 < nch && (since_fold + 1) * CH > kFoldParticles) {
       __syncthreads();
       T.fold(qc);
       since_fold = 0;
     }
   }
-  for (int sp = 0; sp < 2; ++sp) {  // rows with no particles of a species
-    if ((sp == 0 && nc0 == 0) || (sp == 1 && nct == nc0)) {
-      if (tid == 0) {
-        a.sp[sp].nstay[s] = 0;
-        a.sp[sp].nup[s] = 0;
-        a.sp[sp].ndown[s] = 0;
-      }
-    }
-    const unsigned wa = __reduce_add_sync(kFull, nabs[sp]);
-    const unsigned wr = __reduce_add_sync(kFull, nrem[sp]);
-    if (lane == 0 && (wa | wr)) {
-      atomicAdd(&s_cnt[2 * sp], (unsigned long long)wa);
-      atomicAdd(&s_cnt[2 * sp + 1], (unsigned long long)wr);
-    }
+  if (tid == 0) {
+    S.nstay[s] = c_stay;
+    S.nup[s] = min(c_up, S.stage_cap);
+    S.ndown[s] = min(c_dn, S.stage_cap);
+  }
+  const unsigned wa = __reduce_add_sync(kFull, nabs);
+  const unsigned wr = __reduce_add_sync(kFull, nrem);
+  if (lane == 0 && (wa | wr)) {
+    atomicAdd(&s_cnt[0], (unsigned long long)wa);
+    atomicAdd(&s_cnt[1], (unsigned long long)wr);
   }
   __syncthreads();
-  if (tid < 2) {
-    if (s_cnt[2 * tid]) atomicAdd(&ctl->absorbed[tid], s_cnt[2 * tid]);
-    if (s_cnt[2 * tid + 1]) atomicAdd(&ctl->removed[tid], s_cnt[2 * tid + 1]);
+  if (tid == 0) {
+    if (s_cnt[0]) atomicAdd(&ctl->absorbed[sp], s_cnt[0]);
+    if (s_cnt[1]) atomicAdd(&ctl->removed[sp], s_cnt[1]);
   }
-  T.fold(nct > nc0 ? 1 : -1);  // the moments hold the last species' particles
+  T.fold(qc);
   fl = __reduce_or_sync(kFull, fl);
   if (lane == 0) raise_flags(ctl, fl);
 }
 
+// block 2s + sp pushes species sp of row s: both species of a row are
+// independent units of equal size, which halves the tail of the last wave
 __global__ void __launch_bounds__(kPB, 3) k_push_deposit(SimArgs a) {
   extern __shared__ __align__(128) unsigned char push_raw[];
-  push_row<kPB>(a, blockIdx.x, push_raw);
+  push_unit<kPB>(a, blockIdx.x >> 1, blockIdx.x & 1, push_raw);
 }
 
-// many contexts in one launch: work[b] = {instance, row}; PB = 256 for
-// short rows (more blocks per SM), 512 otherwise
+// many contexts in one launch: block 2b + sp pushes species sp of work[b] =
+// {instance, row}; PB = 256 for short rows (more blocks per SM), 512
+// otherwise
 template <int PB>
 __global__ void __launch_bounds__(PB, PB == 256 ? 4 : 2)
     k_push_deposit_batch(const SimArgs *__restrict__ inst, const int2 *__restrict__ work) {
@@ -455,13 +434,13 @@ __global__ void __launch_bounds__(PB, PB == 256 ? 4 : 2)
   // the instance's arguments in shared memory: read there as needed instead
   // of held in registers
   __shared__ __align__(16) SimArgs sa;
-  const int2 w = work[blockIdx.x];
+  const int2 w = work[blockIdx.x >> 1];
   static_assert(sizeof(SimArgs) % 4 == 0, "");
   const unsigned *src = reinterpret_cast<const unsigned *>(inst + w.x);
   unsigned *dst = reinterpret_cast<unsigned *>(&sa);
   for (int k = threadIdx.x; k < (int)(sizeof(SimArgs) / 4); k += PB) dst[k] = src[k];
   __syncthreads();
-  push_row<PB>(sa, w.y, push_raw);
+  push_unit<PB>(sa, w.y, blockIdx.x & 1, push_raw);
 }
 
 // ---------------------------------------------------------------------------
@@ -749,7 +728,7 @@ cudaError_t push_set_smem(size_t bytes) {
 
 cudaError_t launch_push_deposit(const SimArgs &a, cudaStream_t st) {
   const size_t sm = push_smem_bytes(a.nnx, kPB);
-  k_push_deposit<<<a.ncy, kPB, sm, st>>>(a);
+  k_push_deposit<<<2 * a.ncy, kPB, sm, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -796,7 +775,7 @@ cudaError_t push_batch(const SimArgs *inst, const int2 *row_work, int n, int max
     if (e != cudaSuccess) return e;
     cur = sm;
   }
-  k_push_deposit_batch<PB><<<n, PB, sm, st>>>(inst, row_work);
+  k_push_deposit_batch<PB><<<2 * n, PB, sm, st>>>(inst, row_work);
   return cudaGetLastError();
 }
 
