@@ -253,7 +253,11 @@ struct TuneKey {
   }
 };
 std::mutex g_tune_mu;
-std::map<TuneKey, std::pair<int, int>> g_tuned;  // -> (G, K)
+struct TunePick {
+  int G, K;
+  bool nostrip;
+};
+std::map<TuneKey, TunePick> g_tuned;
 
 int tune_jacobi(cupic_ctx *c, int P, long long rows_fit) {
   const int M = c->a.nny - 2;
@@ -264,12 +268,15 @@ int tune_jacobi(cupic_ctx *c, int P, long long rows_fit) {
     std::lock_guard<std::mutex> lk(g_tune_mu);
     auto it = g_tuned.find(key);
     if (it != g_tuned.end()) {
-      const int G = it->second.first, K = it->second.second;
+      const int G = it->second.G, K = it->second.K;
       const int B = jacobi_rows(c, G, K, P, rows_fit);
+      c->jNoStrip = it->second.nostrip;
       if (B) return set_jacobi_plan(c, G, B, K, P);
     }
   }
-  struct Cand { int G, B, K; };
+  // every layout is timed with the sweep form it would get, and again with
+  // the shared-memory sweep where that form is register strips
+  struct Cand { int G, B, K; bool nostrip; };
   std::vector<Cand> cands;
   const int ns = c->num_sms;
   const int gs[] = {1, 2, 4, 8, 16, 24, ns / 4, ns / 2, ns};
@@ -283,10 +290,11 @@ int tune_jacobi(cupic_ctx *c, int P, long long rows_fit) {
     while (kmax > 1 && !jacobi_rows(c, G, kmax, P, rows_fit)) --kmax;
     for (int K : {1, 2, 4, 8, 16, kmax}) {
       if (K > kmax) continue;
-      if (!cands.empty() && cands.back().G == G && cands.back().K >= K) continue;
+      if (!cands.empty() && cands.back().G == G && cands.back().K >= K) continue;  // no repeats
       const int B = jacobi_rows(c, G, K, P, rows_fit);
       if (!B) continue;
-      cands.push_back({G, B, K});
+      cands.push_back({G, B, K, false});
+      if (jacobi_strip_rows(c->a.nnx, B + 2 * (G > 1 ? K : 1) - 2) > 0) cands.push_back({G, B, K, true});
       maxG = std::max(maxG, G);
       maxGK = std::max(maxGK, (long long)G * K);
     }
@@ -304,6 +312,7 @@ int tune_jacobi(cupic_ctx *c, int P, long long rows_fit) {
     c->jB = cd.B;
     c->jK = cd.G > 1 ? cd.K : 1;
     c->jP = P;
+    c->jNoStrip = cd.nostrip;
     JacobiArgs J = jargs(c, 0.0, S, S, chk, 1);
     J.write_stats = 0;
     float t = 1e30f;
@@ -332,8 +341,9 @@ int tune_jacobi(cupic_ctx *c, int P, long long rows_fit) {
   CU(cudaStreamSynchronize(c->stream));
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tuned[key] = {pick.G, pick.K};
+    g_tuned[key] = {pick.G, pick.K, pick.nostrip};
   }
+  c->jNoStrip = pick.nostrip;
   return set_jacobi_plan(c, pick.G, pick.B, pick.K, P);
 }
 
@@ -362,7 +372,7 @@ JacobiArgs jargs(const cupic_ctx *c, double tol, int mn, int mx, int chk, int fi
   J.vec = ((c->a.nnx - 1) % 4 == 0) ? 1 : 0;
   J.strip = jacobi_strip_rows(c->a.nnx, c->jB + 2 * (c->jG > 1 ? c->jK : 1) - 2);
   if (getenv("CUPIC_JACOBI_SCALAR")) J.vec = 0;
-  if (getenv("CUPIC_JACOBI_SCALAR") || getenv("CUPIC_JACOBI_NOSTRIP")) J.strip = 0;
+  if (c->jNoStrip || getenv("CUPIC_JACOBI_SCALAR") || getenv("CUPIC_JACOBI_NOSTRIP")) J.strip = 0;
   J.do_field = field;
   J.write_stats = 1;
   J.flags = c->jflags;

@@ -26,6 +26,7 @@ struct cupic_ctx {
   int64_t total_cap[2] = {0, 0};
   // Jacobi geometry and exchange buffers
   int jG = 1, jB = 1, jK = 1, jP = 0;
+  bool jNoStrip = false;  // the tuner found the shared-memory sweep faster than register strips
   unsigned *jflags = nullptr;  // [G+1]: per-CTA sweep counters, then the barrier
   float *jres = nullptr;
   float *jhalo = nullptr;
