@@ -42,7 +42,7 @@ EXPORTED = [
     "cupic_write_bins_file", "cupic_rewrite_input_data", "cupic_particles_snapshot",
     "cupic_mesh_snapshot", "cupic_save_bm", "cupic_save_bins", "cupic_load_particles_file",
     "cupic_batch_create", "cupic_batch_set", "cupic_batch_step", "cupic_batch_sync",
-    "cupic_batch_destroy",
+    "cupic_batch_destroy", "cupic_probe_current", "cupic_density_profile",
 ]
 
 
@@ -130,6 +130,8 @@ def load_library(build_if_missing=False):
         "cupic_batch_step": [vp, c_i32],
         "cupic_batch_sync": [vp],
         "cupic_batch_destroy": [vp],
+        "cupic_probe_current": [vp, c_i32, P(c_d)],
+        "cupic_density_profile": [vp, c_i, P(c_d)],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -380,6 +382,19 @@ class Sim:
         arr = (StepStats * count)()
         _ok(self.L.cupic_get_stats(self.h, arr, count), "get_stats")
         return [s.as_dict() for s in arr]
+
+    def probe_current(self, window):
+        """Net charge absorbed by the probe per step over the last `window` steps."""
+        v = ctypes.c_double()
+        _ok(self.L.cupic_probe_current(self.h, window, ctypes.byref(v)), "probe_current")
+        return v.value
+
+    def density_profile(self, species):
+        """Particles per unit volume in each cell row (ncy values)."""
+        o = np.empty(self.p.ncy)
+        _ok(self.L.cupic_density_profile(self.h, species, _ptr(o, ctypes.c_double)),
+            "density_profile")
+        return o
 
     def flags(self):
         f = ctypes.c_uint32()

@@ -1248,15 +1248,40 @@ int cupic_get_field(cupic_ctx *c, double *ex, double *ey) {
 
 int cupic_get_stats(cupic_ctx *c, cupic_step_stats *out, int32_t count) {
   if (!c || !out || count < 0 || count > kStatsRing) return CUPIC_ERR_ARG;
+  if (count == 0) return CUPIC_OK;
   CU(cudaSetDevice(c->device));
   CU(cudaStreamSynchronize(c->stream));
   int64_t step = 0;
   CU(cudaMemcpy(&step, &c->ctl->step, sizeof(step), cudaMemcpyDeviceToHost));
-  for (int32_t k = 0; k < count; ++k) {
-    const int64_t s = step - count + k;
-    const int64_t idx = ((s % kStatsRing) + kStatsRing) % kStatsRing;
-    CU(cudaMemcpy(&out[k], &c->ctl->ring[idx], sizeof(cupic_step_stats), cudaMemcpyDeviceToHost));
-  }
+  // the ring entries of steps step-count .. step-1, in at most two copies
+  const int64_t first = (((step - count) % kStatsRing) + kStatsRing) % kStatsRing;
+  const int64_t n1 = std::min<int64_t>(count, kStatsRing - first);
+  CU(cudaMemcpy(out, &c->ctl->ring[first], n1 * sizeof(cupic_step_stats), cudaMemcpyDeviceToHost));
+  if (n1 < count)
+    CU(cudaMemcpy(out + n1, &c->ctl->ring[0], (count - n1) * sizeof(cupic_step_stats),
+                  cudaMemcpyDeviceToHost));
+  return CUPIC_OK;
+}
+
+int cupic_probe_current(cupic_ctx *c, int32_t window, double *current) {
+  if (!c || !current || window < 1 || window > kStatsRing) return CUPIC_ERR_ARG;
+  std::vector<cupic_step_stats> st(window);
+  int rc = cupic_get_stats(c, st.data(), window);
+  if (rc) return rc;
+  double sum = 0.0;
+  for (const cupic_step_stats &x : st)
+    sum += c->p.qe * (double)x.absorbed[0] + c->p.qi * (double)x.absorbed[1];
+  *current = sum / window;
+  return CUPIC_OK;
+}
+
+int cupic_density_profile(cupic_ctx *c, int species, double *density) {
+  if (!c || !density || species < 0 || species > 1) return CUPIC_ERR_ARG;
+  std::vector<int32_t> cnt;
+  int rc = get_row_counts(c, species, cnt);
+  if (rc) return rc;
+  const double cell = c->p.ds * c->p.ds * c->p.ds;
+  for (int j = 0; j < c->p.ncy; ++j) density[j] = cnt[j] / (c->p.ncx * cell);
   return CUPIC_OK;
 }
 

@@ -48,8 +48,7 @@ def poisson_arrivals(n, rate, seed=3):
 
 
 def probe_current(sim, window):
-    st = sim.stats(window)
-    return float(np.mean([s["absorbed"][1] - s["absorbed"][0] for s in st]))
+    return sim.probe_current(window)
 
 
 def warm_plans(requests, device=0):

@@ -230,6 +230,13 @@ int cupic_get_field_f32(struct cupic_ctx *ctx, float *ex, float *ey);
 /* Stats of the last `count` steps (most recent last). */
 int cupic_get_stats(struct cupic_ctx *ctx, cupic_step_stats *out, int32_t count);
 int cupic_get_flags(struct cupic_ctx *ctx, uint32_t *flags);
+/* Probe current: the net charge absorbed by the probe per step (qe times the
+ * electrons plus qi times the ions crossing y<0), averaged over the last
+ * `window` steps (at most 4096). */
+int cupic_probe_current(struct cupic_ctx *ctx, int32_t window, double *current);
+/* Density profile of one species: particles per unit volume in each cell
+ * row, count / (ncx ds^3), ncy values; the initial plasma gives n. */
+int cupic_density_profile(struct cupic_ctx *ctx, int species, double *density);
 int cupic_clear_flags(struct cupic_ctx *ctx);
 
 /* ---- solve without allocating ------------------------------------------ */

@@ -193,3 +193,17 @@ def test_small_workload_matches_committed_golden(gpu_lib):
             assert {key: st[key] for key in gold["stats"][k - 1]} == gold["stats"][k - 1], k
             if k in (1, 10):
                 assert snap() == gold["states"][f"step{k}"], k
+
+
+def test_probe_current_and_density_diagnostics(gpu_lib):
+    p = cg.workload_params("small")
+    with cg.Sim(p) as sim:
+        sim.init_plasma()
+        for sp in (0, 1):
+            np.testing.assert_array_equal(sim.density_profile(sp), np.full(p.ncy, p.n))
+        sim.step(12)
+        st = sim.stats(10)
+        want = np.mean([p.qe * s["absorbed"][0] + p.qi * s["absorbed"][1] for s in st])
+        assert sim.probe_current(10) == pytest.approx(want, rel=0, abs=1e-12)
+        rows = sim.row_counts(1)
+        np.testing.assert_allclose(sim.density_profile(1), rows / (p.ncx * p.ds ** 3), rtol=1e-15)
