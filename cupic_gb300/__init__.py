@@ -43,6 +43,7 @@ EXPORTED = [
     "cupic_mesh_snapshot", "cupic_save_bm", "cupic_save_bins", "cupic_load_particles_file",
     "cupic_batch_create", "cupic_batch_set", "cupic_batch_step", "cupic_batch_sync",
     "cupic_batch_destroy", "cupic_probe_current", "cupic_density_profile",
+    "cupic_test_bounded_wait",
 ]
 
 
@@ -132,6 +133,7 @@ def load_library(build_if_missing=False):
         "cupic_batch_destroy": [vp],
         "cupic_probe_current": [vp, c_i32, P(c_d)],
         "cupic_density_profile": [vp, c_i, P(c_d)],
+        "cupic_test_bounded_wait": [vp],
     }
     for name, args in sig.items():
         fn = getattr(L, name)

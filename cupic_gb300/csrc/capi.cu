@@ -1292,6 +1292,13 @@ int cupic_get_flags(cupic_ctx *c, uint32_t *flags) {
   return read_ctl_flags(c, flags);
 }
 
+int cupic_test_bounded_wait(cupic_ctx *c) {
+  if (!c) return CUPIC_ERR_ARG;
+  CU(cudaSetDevice(c->device));
+  CU(launch_wait_probe(c->a, c->stream));
+  return finish(c);
+}
+
 int cupic_clear_flags(cupic_ctx *c) {
   if (!c) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));

@@ -537,6 +537,18 @@ cudaError_t jacobi_max_ctas(size_t smem, int *per_sm) {
   return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_jacobi, kJBlock, smem);
 }
 
+// Fault-detection self-test: one thread waits, through the solver's bounded
+// wait, on a word of the control block that nothing writes.  The wait gives
+// up after its iteration limit and raises CUPIC_FLAG_TIMEOUT.
+__global__ void k_wait_probe(SimArgs a) {
+  if (threadIdx.x == 0) wait_geq(reinterpret_cast<const unsigned *>(&a.ctl->pad), 1u, a.ctl);
+}
+
+cudaError_t launch_wait_probe(const SimArgs &a, cudaStream_t st) {
+  k_wait_probe<<<1, 32, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
 cudaError_t jacobi_batch_set_smem(size_t bytes) {
   static size_t cur = 48 * 1024;
   if (bytes <= cur) return cudaSuccess;

@@ -52,6 +52,9 @@ cudaError_t launch_inject_draw_batch(const SimArgs *inst, int n, int max_inj_cap
 cudaError_t launch_inject_append_batch(const SimArgs *inst, int n, int max_ncy, cudaStream_t st);
 cudaError_t launch_finalize_batch(const SimArgs *inst, int n, cudaStream_t st);
 
+// fault-detection self-test (jacobi.cu)
+cudaError_t launch_wait_probe(const SimArgs &a, cudaStream_t st);
+
 // precision form of the solve (refine.cu)
 cudaError_t launch_r64_residual(const SimArgs &a, const double *phi64, float *rr, float *dl,
                                 unsigned long long *maxr, cudaStream_t st);

@@ -238,6 +238,12 @@ int cupic_probe_current(struct cupic_ctx *ctx, int32_t window, double *current);
  * row, count / (ncx ds^3), ncy values; the initial plasma gives n. */
 int cupic_density_profile(struct cupic_ctx *ctx, int species, double *density);
 int cupic_clear_flags(struct cupic_ctx *ctx);
+/* Fault-detection self-test, with no counterpart in the reference: one GPU
+ * thread waits, through the solver's bounded wait, on a word that nothing
+ * writes.  The wait gives up after its limit (under a second), raises
+ * CUPIC_FLAG_TIMEOUT and the kernel returns; the call returns
+ * CUPIC_ERR_TIMEOUT.  cupic_clear_flags makes the context usable again. */
+int cupic_test_bounded_wait(struct cupic_ctx *ctx);
 
 /* ---- solve without allocating ------------------------------------------ */
 
