@@ -54,7 +54,9 @@ struct RhoMoments {
   unsigned long long *g;
 
   __device__ __forceinline__ void deposit(const SimArgs &a, float x, float y, int q) const {
-    const CicFixed c = cic_fixed(a, x, y);
+    deposit(cic_fixed(a, x, y), q);
+  }
+  __device__ __forceinline__ void deposit(const CicFixed &c, int q) const {
     const int tr = c.jc - crow0;
     if (tr >= 0 && tr < ncr) {
       unsigned *mc = m + kMomStride * (tr * ncx + c.ic);
@@ -127,6 +129,38 @@ __device__ __forceinline__ Cls classify(const SimArgs &a, const float4 &p, int s
   const int d = row_of(a, p.y);
   if (s >= 0 && (d > s + 1 || d < s - 1)) return {s, f | CUPIC_FLAG_CFL};
   return {d, f};
+}
+
+// A pushed particle of row s: classify() and, if it stays in the row set,
+// deposit it; returns 0 stay, 1 up, 2 down, 3 absorbed or removed.
+// Fast path: x = wrap(x0 + dt vx) and y = y0 + dt vy are finite only if vx
+// and vy are (dt = 0 turns an infinite velocity into NaN), so a particle
+// with both coordinates inside the domain is finite4 and needs no further
+// test but the row step; its row is the deposit's cell row.
+__device__ __forceinline__ int settle(const SimArgs &a, const float4 &v, int s, const RhoMoments &T,
+                                      int q, uint32_t &fl, unsigned &nabs, unsigned &nrem) {
+  if (v.y >= 0.0f && v.y < a.Ly && v.x >= 0.0f && v.x < a.Lx) {
+    const CicFixed c = cic_fixed(a, v.x, v.y);
+    T.deposit(c, q);
+    const int dj = c.jc - s;  // c.jc == row_of(a, v.y)
+    if (dj == 0) return 0;
+    if (dj == 1) return 1;
+    if (dj == -1) return 2;
+    fl |= CUPIC_FLAG_CFL;
+    return 0;
+  }
+  const Cls c = classify(a, v, s);
+  fl |= c.flag;
+  if (c.dest == kRowAbsorbed) {
+    ++nabs;
+    return 3;
+  }
+  if (c.dest == kRowRemoved) {
+    ++nrem;
+    return 3;
+  }
+  T.deposit(a, v.x, v.y, q);
+  return c.dest == s ? 0 : (c.dest == s + 1 ? 1 : 2);
 }
 
 }  // namespace
@@ -328,26 +362,19 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
         v.x = __fmaf_rn(a.dt, v.z, v.x);
         v.y = __fmaf_rn(a.dt, v.w, v.y);
         v.x = wrap_x(a, v.x);
-        const Cls c = classify(a, v, s);
-        fl |= c.flag;
-        if (c.dest == kRowAbsorbed) {
-          ++nabs;
-        } else if (c.dest == kRowRemoved) {
-          ++nrem;
-        } else {
-          cat[j] = c.dest == s ? 0 : (c.dest == s + 1 ? 1 : 2);
-        }
+        cat[j] = settle(a, v, s, T, qc, fl, nabs, nrem);
         p[j] = v;
       }
     }
-    uint32_t bs[kPPT], bu[kPPT], bd[kPPT];
+    // category bits of the warp's lanes: 00 stay, 01 up, 10 down, 11 none
+    uint32_t b0[kPPT], b1[kPPT];
     uint32_t *ws = wsum[k & 1];
 #pragma unroll
     for (int j = 0; j < kPPT; ++j) {
-      bs[j] = __ballot_sync(kFull, cat[j] == 0);
-      bu[j] = __ballot_sync(kFull, cat[j] == 1);
-      bd[j] = __ballot_sync(kFull, cat[j] == 2);
-      if (lane == 0) ws[j * NW + warp] = pack3(__popc(bs[j]), __popc(bu[j]), __popc(bd[j]));
+      b0[j] = __ballot_sync(kFull, cat[j] & 1);
+      b1[j] = __ballot_sync(kFull, cat[j] & 2);
+      if (lane == 0)
+        ws[j * NW + warp] = pack3(__popc(~(b0[j] | b1[j])), __popc(b0[j] & ~b1[j]), __popc(b1[j] & ~b0[j]));
     }
     __syncthreads();  // the only block barrier of a chunk
     // every thread holds its particles: refill this stage with chunk k+kStages
@@ -357,42 +384,39 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
       mbar_arrive_expect_tx(&full[st], (uint32_t)cnt2 * 16u);
       bulk_g2s(stage + st * CH, row + (size_t)k2 * CH, (uint32_t)cnt2 * 16u, &full[st]);
     }
-    // Every warp scans the chunk's NE entries itself (no second barrier).
-    // Exclusive prefixes are at most 32*(NE-1) < 1024 per field, so the
-    // packed sums never carry between fields; the chunk totals come from the
-    // last entry field by field.
+    // Every warp sums the chunk's NE entries itself (no second barrier): the
+    // exclusive prefix of entry e is the sum of entries 0..e-1.  Exclusive
+    // prefixes are at most 32*(NE-1) < 1024 per field, so the packed sums
+    // never carry between fields; the chunk totals come from the last entry
+    // field by field.
     const uint32_t v = lane < NE ? ws[lane] : 0u;
-    uint32_t inc = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t u = __shfl_up_sync(kFull, inc, o);
-      if (lane >= o) inc += u;
-    }
-    const uint32_t ex = inc - v;
-    const uint32_t exl = __shfl_sync(kFull, ex, NE - 1), vl = __shfl_sync(kFull, v, NE - 1);
+    const uint32_t exl = __reduce_add_sync(kFull, lane < NE - 1 ? v : 0u);
+    const uint32_t vl = __shfl_sync(kFull, v, NE - 1);
 #pragma unroll
     for (int j = 0; j < kPPT; ++j) {
-      const uint32_t off = __shfl_sync(kFull, ex, j * NW + warp);
-      if (cat[j] == 0) {
-        row[c_stay + (int)field0(off) + __popc(bs[j] & lt)] = p[j];
-      } else if (cat[j] == 1) {
-        const int pos = c_up + (int)field1(off) + __popc(bu[j] & lt);
-        if (pos < S.stage_cap) sup[pos] = p[j]; else fl |= CUPIC_FLAG_STAGE;
-      } else if (cat[j] == 2) {
-        const int pos = c_dn + (int)field2(off) + __popc(bd[j] & lt);
-        if (pos < S.stage_cap) sdn[pos] = p[j]; else fl |= CUPIC_FLAG_STAGE;
+      const uint32_t off = __reduce_add_sync(kFull, lane < j * NW + warp ? v : 0u);
+      const int c = cat[j];
+      if (c < 3) {
+        // one store: the slot among the lanes of the same category
+        const uint32_t m0 = (c & 1) ? kFull : 0u, m1 = (c & 2) ? kFull : 0u;
+        const uint32_t same = ~((b0[j] ^ m0) | (b1[j] ^ m1));
+        const int sh = c == 0 ? 0 : (c == 1 ? 10 : 21);
+        const int base = c == 0 ? c_stay : (c == 1 ? c_up : c_dn);
+        const int pos = base + (int)((off >> sh) & (c == 0 ? 0x3ffu : 0x7ffu)) + __popc(same & lt);
+        float4 *dst = c == 0 ? row : (c == 1 ? sup : sdn);
+        if (c == 0 || pos < S.stage_cap) dst[pos] = p[j]; else fl |= CUPIC_FLAG_STAGE;
       }
-      if (cat[j] < 3) T.deposit(a, p[j].x, p[j].y, qc);
     }
     c_stay += (int)(field0(exl) + field0(vl));
     c_up += (int)(field1(exl) + field1(vl));
     c_dn += (int)(field2(exl) + field2(vl));
-    // fold before the moments could overflow (block-uniform); the next
-    // deposits follow the next chunk's barrier
+    // fold before the moments could overflow (block-uniform); the barrier
+    // after it orders the clearing before the next chunk's deposits
     ++since_fold;
     if (k + 1 < nch && (since_fold + 1) * CH > kFoldParticles) {
       __syncthreads();
       T.fold(qc);
+      __syncthreads();
       since_fold = 0;
     }
   }
