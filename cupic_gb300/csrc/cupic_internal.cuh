@@ -223,51 +223,23 @@ __device__ __forceinline__ void dev_sincos2pi(double u, double *s, double *c) {
 // rows s and s+1 (tile row stride = nnx).
 __device__ __forceinline__ void gather_tile(const SimArgs &a, const float2 *tile, float x, float y,
                                             int s, float &Epx, float &Epy) {
-  const float sx = __fmul_rn(x, a.inv_ds);
-  const int ic = cfloorf(sx, 0, a.ncx - 1);
-  const float fx = clamp01f(__fsub_rn(sx, (float)ic));
-  const float fy = clamp01f(__fsub_rn(__fmul_rn(y, a.inv_ds), (float)s));
-  const float gx = __fsub_rn(1.0f, fx), gy = __fsub_rn(1.0f, fy);
-  const float w00 = __fmul_rn(gx, gy), w10 = __fmul_rn(fx, gy);
-  const float w01 = __fmul_rn(gx, fy), w11 = __fmul_rn(fx, fy);
+  // x and y components side by side in packed FP32x2 operations; each
+  // component is rounded exactly as its scalar operation
+  const float2 sxy = __fmul2_rn(make_float2(x, y), make_float2(a.inv_ds, a.inv_ds));
+  const int ic = cfloorf(sxy.x, 0, a.ncx - 1);
+  const float2 d = __fadd2_rn(sxy, make_float2(-(float)ic, -(float)s));  // sx - ic, sy - s
+  const float fx = clamp01f(d.x), fy = clamp01f(d.y);
+  const float2 g = __fadd2_rn(make_float2(1.0f, 1.0f), make_float2(-fx, -fy));  // gx, gy
+  const float2 wlo = __fmul2_rn(make_float2(g.x, fx), make_float2(g.y, g.y));    // w00, w10
+  const float2 whi = __fmul2_rn(make_float2(g.x, fx), make_float2(fy, fy));      // w01, w11
   const float2 e00 = tile[ic], e10 = tile[ic + 1];
   const float2 e01 = tile[a.nnx + ic], e11 = tile[a.nnx + ic + 1];
-  float ex = __fmul_rn(w00, e00.x);
-  ex = __fmaf_rn(w10, e10.x, ex);
-  ex = __fmaf_rn(w01, e01.x, ex);
-  ex = __fmaf_rn(w11, e11.x, ex);
-  float ey = __fmul_rn(w00, e00.y);
-  ey = __fmaf_rn(w10, e10.y, ey);
-  ey = __fmaf_rn(w01, e01.y, ey);
-  ey = __fmaf_rn(w11, e11.y, ey);
-  Epx = ex;
-  Epy = ey;
-}
-
-// CIC field from a shared tile of node pairs: tile4[r*ncx + i] =
-// {Ex(i), Ey(i), Ex(i+1), Ey(i+1)} of node row s+r, so a particle's four
-// nodes come in two 16-byte loads.  Same operations, in the same order, as
-// gather_tile.
-__device__ __forceinline__ void gather_tile4(const SimArgs &a, const float4 *tile4, float x, float y,
-                                             int s, float &Epx, float &Epy) {
-  const float sx = __fmul_rn(x, a.inv_ds);
-  const int ic = cfloorf(sx, 0, a.ncx - 1);
-  const float fx = clamp01f(__fsub_rn(sx, (float)ic));
-  const float fy = clamp01f(__fsub_rn(__fmul_rn(y, a.inv_ds), (float)s));
-  const float gx = __fsub_rn(1.0f, fx), gy = __fsub_rn(1.0f, fy);
-  const float w00 = __fmul_rn(gx, gy), w10 = __fmul_rn(fx, gy);
-  const float w01 = __fmul_rn(gx, fy), w11 = __fmul_rn(fx, fy);
-  const float4 lo = tile4[ic], hi = tile4[a.ncx + ic];
-  float ex = __fmul_rn(w00, lo.x);
-  ex = __fmaf_rn(w10, lo.z, ex);
-  ex = __fmaf_rn(w01, hi.x, ex);
-  ex = __fmaf_rn(w11, hi.z, ex);
-  float ey = __fmul_rn(w00, lo.y);
-  ey = __fmaf_rn(w10, lo.w, ey);
-  ey = __fmaf_rn(w01, hi.y, ey);
-  ey = __fmaf_rn(w11, hi.w, ey);
-  Epx = ex;
-  Epy = ey;
+  float2 e = __fmul2_rn(make_float2(wlo.x, wlo.x), e00);
+  e = __ffma2_rn(make_float2(wlo.y, wlo.y), e10, e);
+  e = __ffma2_rn(make_float2(whi.x, whi.x), e01, e);
+  e = __ffma2_rn(make_float2(whi.y, whi.y), e11, e);
+  Epx = e.x;
+  Epy = e.y;
 }
 
 // fixed-point CIC weights: 16 fractional bits per axis and the cross term
@@ -282,14 +254,13 @@ struct CicFixed {
 
 __device__ __forceinline__ CicFixed cic_fixed(const SimArgs &a, float x, float y) {
   CicFixed r;
-  const float sx = __fmul_rn(x, a.inv_ds);
-  r.ic = cfloorf(sx, 0, a.ncx - 1);
-  const float fx = clamp01f(__fsub_rn(sx, (float)r.ic));
-  const float sy = __fmul_rn(y, a.inv_ds);
-  r.jc = cfloorf(sy, 0, a.ncy - 1);
-  const float fy = clamp01f(__fsub_rn(sy, (float)r.jc));
-  r.FX = __float2int_rn(__fmul_rn(fx, 65536.0f));
-  r.FY = __float2int_rn(__fmul_rn(fy, 65536.0f));
+  const float2 sxy = __fmul2_rn(make_float2(x, y), make_float2(a.inv_ds, a.inv_ds));
+  r.ic = cfloorf(sxy.x, 0, a.ncx - 1);
+  r.jc = cfloorf(sxy.y, 0, a.ncy - 1);
+  const float2 d = __fadd2_rn(sxy, make_float2(-(float)r.ic, -(float)r.jc));
+  const float2 f = __fmul2_rn(make_float2(clamp01f(d.x), clamp01f(d.y)), make_float2(65536.0f, 65536.0f));
+  r.FX = __float2int_rn(f.x);
+  r.FY = __float2int_rn(f.y);
   r.FXY = (int)(((unsigned long long)r.FX * (unsigned long long)r.FY + 32768ull) >> 16);
   const long long FX = r.FX, FY = r.FY, W11 = (long long)r.FXY << 16;
   r.w11 = W11;

@@ -18,7 +18,7 @@ cudaError_t launch_inject(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_inject_draw(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_inject_append(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_finalize(const SimArgs &a, cudaStream_t st);
-size_t push_smem_bytes(int nnx, int pb = 512);
+size_t push_smem_bytes(int nnx, int pb = 256);  // pb: threads per block (256 single context)
 cudaError_t push_set_smem(size_t bytes);
 
 int load_blocks(int64_t n, int num_sms);

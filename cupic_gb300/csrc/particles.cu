@@ -260,8 +260,8 @@ __global__ void k_leapfrog_start(SimArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// fused push + wrap + row binning + deposition, one block per cell row s
-// handling both species (particles.cu:110-231, cc.cu:303-810, mesh.cu:162-293)
+// fused push + wrap + row binning + deposition, one block per (cell row s,
+// species) unit (particles.cu:110-231, cc.cu:303-810, mesh.cu:162-293)
 //
 // The row's particles stream through a ring of kStages shared-memory chunks
 // of CH = PB*PPT particles filled by 1-D bulk copies (TMA) that run
@@ -273,7 +273,7 @@ __global__ void k_leapfrog_start(SimArgs a) {
 // and every later chunk is disjoint from it.
 // ---------------------------------------------------------------------------
 namespace {
-constexpr int kPB = 512;       // threads (single context; batched short rows use 256)
+constexpr int kPB = 256;       // threads of the single-context push (4 blocks per SM)
 constexpr int kPPT = 2;        // particles per thread per chunk
 constexpr int kStages = 2;     // chunks in flight
 // a chunk's scan has one entry per (particle slot j, warp), 32 particles each
@@ -357,11 +357,10 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
         float4 v = stage[st * CH + idx];
         float ex, ey;
         gather_tile(a, etile, v.x, v.y, s, ex, ey);
-        v.z = __fmaf_rn(dtqm, ex, v.z);
-        v.w = __fmaf_rn(dtqm, ey, v.w);
-        v.x = __fmaf_rn(a.dt, v.z, v.x);
-        v.y = __fmaf_rn(a.dt, v.w, v.y);
-        v.x = wrap_x(a, v.x);
+        // v += dtqm E, then r += dt v, both components per packed operation
+        const float2 vel = __ffma2_rn(make_float2(dtqm, dtqm), make_float2(ex, ey), make_float2(v.z, v.w));
+        const float2 pos = __ffma2_rn(make_float2(a.dt, a.dt), vel, make_float2(v.x, v.y));
+        v = make_float4(wrap_x(a, pos.x), pos.y, vel.x, vel.y);
         cat[j] = settle(a, v, s, T, qc, fl, nabs, nrem);
         p[j] = v;
       }
@@ -443,7 +442,7 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
 
 // block 2s + sp pushes species sp of row s: both species of a row are
 // independent units of equal size, which halves the tail of the last wave
-__global__ void __launch_bounds__(kPB, 3) k_push_deposit(SimArgs a) {
+__global__ void __launch_bounds__(kPB, 4) k_push_deposit(SimArgs a) {
   extern __shared__ __align__(128) unsigned char push_raw[];
   push_unit<kPB>(a, blockIdx.x >> 1, blockIdx.x & 1, push_raw);
 }
