@@ -156,10 +156,13 @@ __device__ __forceinline__ float sweep_scalar(const float *__restrict__ S, float
 // source terms.  A sweep then reads from shared memory only the rows just
 // below and above the strip and the west/east values at the ends of a warp
 // or a row; the strip's own rows come from registers and its west/east
-// neighbours by shuffle.  Every updated row is still stored to D, where the
-// neighbouring strips, lanes and the halo exchange find it.  Rows outside
-// [u0, u1) keep their registers unchanged, exactly as the shared-memory
-// path leaves them unwritten.
+// neighbours by shuffle.  D receives only what other threads read: the
+// strip's first and last rows (the neighbouring strips' south and north
+// rows) and, of the rows between, the values at the ends of a warp's span
+// and the seam columns -- every updated row in full only when `full` (the
+// sweep before a halo exchange).  Rows outside [u0, u1) keep their
+// registers unchanged, exactly as the shared-memory path leaves them
+// unwritten.
 struct RegGeom {
   int P, W, NG, gx, gy, lane, lr0, nvalid, col, lcol;
   bool active, lfix, rfix, seam;
@@ -170,7 +173,7 @@ __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cas
 template <int R, bool CHECK>
 __device__ __forceinline__ float sweep_reg(float4 (&x)[R], const float4 (&b)[R], const float *__restrict__ S,
                                            float *__restrict__ D, const RegGeom &g, int u0, int u1, int o0,
-                                           int o1) {
+                                           int o1, bool full) {
   const int P = g.P, W = g.W, col = g.col;
   float4 s4 = make_float4(0.f, 0.f, 0.f, 0.f), n4 = s4;
   if (g.active && g.nvalid > 0) {
@@ -198,7 +201,12 @@ __device__ __forceinline__ float sweep_reg(float4 (&x)[R], const float4 (&b)[R],
         v.z = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].z, c.y), c.w), nb.z), prev.z));
         v.w = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].w, c.z), rt), nb.w), prev.w));
         float *dp = D + lr * P;
-        *reinterpret_cast<float4 *>(dp + col) = v;
+        if (full || r == 0 || r == g.nvalid - 1) {
+          *reinterpret_cast<float4 *>(dp + col) = v;
+        } else {
+          if (g.lfix) dp[col] = v.x;      // east neighbour of the lane before
+          if (g.rfix) dp[col + 3] = v.w;  // west neighbour of the lane after (or of column 0)
+        }
         if (g.seam) dp[W] = v.x;
         if (CHECK && lr >= o0 && lr < o1) {
           md = fmaxf(md, fabsf(__fsub_rn(v.x, c.x)));
@@ -305,10 +313,10 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
       }
     }
   }
-  auto sweep = [&](const float *S, float *D, int u0, int u1, bool check) -> float {
+  auto sweep = [&](const float *S, float *D, int u0, int u1, bool check, bool full) -> float {
     if constexpr (R > 0) {
-      return check ? sweep_reg<R, true>(x, bb, S, D, rg, u0, u1, o0, o1)
-                   : sweep_reg<R, false>(x, bb, S, D, rg, u0, u1, o0, o1);
+      return check ? sweep_reg<R, true>(x, bb, S, D, rg, u0, u1, o0, o1, full)
+                   : sweep_reg<R, false>(x, bb, S, D, rg, u0, u1, o0, o1, full);
     } else {
       if (u0 >= u1) return 0.0f;
       if (vec) return check ? sweep_vec<true>(S, D, bsrc, sg, u0, u1, o0, o1)
@@ -360,10 +368,12 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
       }
     }
     __syncthreads();
-    if constexpr (R > 0) {  // the strips' halo rows are new: reload the registers
+    if constexpr (R > 0) {  // the strips' halo rows are new: reload their registers
 #pragma unroll
-      for (int r = 0; r < R; ++r)
-        if (r < rg.nvalid) x[r] = lds4(D + (rg.lr0 + r) * P + rg.col);
+      for (int r = 0; r < R; ++r) {
+        const int lr = rg.lr0 + r;
+        if (r < rg.nvalid && (lr < o0 || lr >= o1)) x[r] = lds4(D + lr * P + rg.col);
+      }
     }
     return true;
   };
@@ -378,23 +388,24 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
     m = (m >= K) ? 1 : m + 1;                        // position in the temporal block
     const int u0 = max(1, r0 - K + m) - lo;          // updated local rows [u0, u1)
     const int u1 = min(nny - 2, r1 - 1 + K - m) + 1 - lo;
+    const bool full = G > 1 && m == K;  // a halo exchange follows this sweep
     float md;
     if (R > 0) {
       if (pending) {
         if (!receive(S, pending)) break;
         pending = 0;
       }
-      md = sweep(S, D, u0, u1, check);
+      md = sweep(S, D, u0, u1, check, full);
     } else if (pending) {
       // rows o0+1 .. o1-2 read only owned rows of S: sweep them first
       const int i0 = max(u0, o0 + 1), i1 = min(u1, o1 - 1);
-      md = sweep(S, D, i0, i1, check);
+      md = sweep(S, D, i0, i1, check, full);
       if (!receive(S, pending)) break;
-      md = fmaxf(md, sweep(S, D, u0, min(i0, u1), check));
-      md = fmaxf(md, sweep(S, D, max(i1, u0), u1, check));
+      md = fmaxf(md, sweep(S, D, u0, min(i0, u1), check, full));
+      md = fmaxf(md, sweep(S, D, max(i1, u0), u1, check, full));
       pending = 0;
     } else {
-      md = sweep(S, D, u0, u1, check);
+      md = sweep(S, D, u0, u1, check, full);
     }
     __syncthreads();
     if (G > 1 && m == K) {
@@ -425,6 +436,21 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
   }
   float *F = src ? buf1 : buf0;
   if (pending && !bail) receive(F, pending);
+  if constexpr (R > 0) {
+    // the strips' rows in full: the rows between a strip's first and last
+    // are current only in registers
+    if (rg.active) {
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (r < rg.nvalid) {
+          float *dp = F + (rg.lr0 + r) * P;
+          *reinterpret_cast<float4 *>(dp + rg.col) = x[r];
+          if (rg.seam) dp[rg.W] = x[r].x;
+        }
+      }
+    }
+    __syncthreads();
+  }
 
   // write back the owned rows; derive E = -grad phi (mesh.cu:413-468).  The
   // rows r0-1 and r1 are current: either just exchanged or updated in the

@@ -112,6 +112,34 @@ def test_multi_cta_jacobi(make_pair, ctas):
     check_state(sim, ora)
 
 
+@pytest.mark.parametrize("name,over,ctas,depth,strips", [
+    ("small", {}, 1, 1, True),
+    ("small", {}, 3, 1, True),
+    ("small", {}, 3, 4, True),
+    ("small", {}, 4, 8, True),
+    ("small", {}, 4, 8, False),
+    ("small", {}, 7, 3, True),
+    ("small", {"ncx": 256, "ncy": 64}, 2, 8, True),
+    ("small", {"ncx": 256, "ncy": 64}, 3, 5, False),
+])
+def test_jacobi_layouts(make_pair, monkeypatch, name, over, ctas, depth, strips):
+    """Every solver layout -- CTA count, temporal-blocking depth, register
+    strips or the shared-memory sweep -- gives the oracle's bits."""
+    monkeypatch.setenv("CUPIC_JACOBI_DEPTH", str(depth))
+    if strips:
+        monkeypatch.delenv("CUPIC_JACOBI_NOSTRIP", raising=False)
+    else:
+        monkeypatch.setenv("CUPIC_JACOBI_NOSTRIP", "1")
+    sim, ora = make_pair(name, ctas=ctas, max_sweeps=300, **over)
+    G, _, K = sim.solver_plan()
+    assert G == ctas and (K == depth or G == 1)
+    sim.init_plasma()
+    ora.init_plasma()
+    sim.step(2)
+    ora.step(2)
+    check_state(sim, ora)
+
+
 def test_stage_api_matches_oracle(make_pair):
     """Drive the reference's entry points one by one on a state loaded from
     host arrays (read_particle_file + the main loop, main.cu:59-96)."""
