@@ -252,13 +252,25 @@ struct CicFixed {
   long long w00, w10, w01, w11;
 };
 
+// INSIDE: the caller knows 0 <= x < Lx and 0 <= y < Ly.  Then the cell
+// indices and the offsets in the cell are >= 0, so of the clamps only the
+// upper ones can act and the others are left out (same results).
+template <bool INSIDE = false>
 __device__ __forceinline__ CicFixed cic_fixed(const SimArgs &a, float x, float y) {
   CicFixed r;
   const float2 sxy = __fmul2_rn(make_float2(x, y), make_float2(a.inv_ds, a.inv_ds));
-  r.ic = cfloorf(sxy.x, 0, a.ncx - 1);
-  r.jc = cfloorf(sxy.y, 0, a.ncy - 1);
+  if (INSIDE) {
+    r.ic = min(__float2int_rd(sxy.x), a.ncx - 1);
+    r.jc = min(__float2int_rd(sxy.y), a.ncy - 1);
+  } else {
+    r.ic = cfloorf(sxy.x, 0, a.ncx - 1);
+    r.jc = cfloorf(sxy.y, 0, a.ncy - 1);
+  }
   const float2 d = __fadd2_rn(sxy, make_float2(-(float)r.ic, -(float)r.jc));
-  const float2 f = __fmul2_rn(make_float2(clamp01f(d.x), clamp01f(d.y)), make_float2(65536.0f, 65536.0f));
+  const float2 f = INSIDE ? __fmul2_rn(make_float2(fminf(d.x, 1.0f), fminf(d.y, 1.0f)),
+                                       make_float2(65536.0f, 65536.0f))
+                          : __fmul2_rn(make_float2(clamp01f(d.x), clamp01f(d.y)),
+                                       make_float2(65536.0f, 65536.0f));
   r.FX = __float2int_rn(f.x);
   r.FY = __float2int_rn(f.y);
   r.FXY = (int)(((unsigned long long)r.FX * (unsigned long long)r.FY + 32768ull) >> 16);

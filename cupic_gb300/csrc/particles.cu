@@ -140,7 +140,7 @@ __device__ __forceinline__ Cls classify(const SimArgs &a, const float4 &p, int s
 __device__ __forceinline__ int settle(const SimArgs &a, const float4 &v, int s, const RhoMoments &T,
                                       int q, uint32_t &fl, unsigned &nabs, unsigned &nrem) {
   if (v.y >= 0.0f && v.y < a.Ly && v.x >= 0.0f && v.x < a.Lx) {
-    const CicFixed c = cic_fixed(a, v.x, v.y);
+    const CicFixed c = cic_fixed<true>(a, v.x, v.y);
     T.deposit(c, q);
     const int dj = c.jc - s;  // c.jc == row_of(a, v.y)
     if (dj == 0) return 0;
@@ -307,7 +307,7 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
   float2 *etile = reinterpret_cast<float2 *>(stage + kStages * CH);  // node rows s, s+1
   unsigned *tmom = reinterpret_cast<unsigned *>(etile + 2 * nnx);      // cell rows s-1..s+1
   __shared__ __align__(8) uint64_t full[kStages];
-  __shared__ uint32_t wsum[2][NE];  // per-entry packed counts, alternate chunks
+  __shared__ uint2 wmask[2][NE];  // per-entry category ballots, alternate chunks
   __shared__ unsigned long long s_cnt[2];
 
   Ctl *ctl = a.ctl;
@@ -367,13 +367,12 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
     }
     // category bits of the warp's lanes: 00 stay, 01 up, 10 down, 11 none
     uint32_t b0[kPPT], b1[kPPT];
-    uint32_t *ws = wsum[k & 1];
+    uint2 *wm = wmask[k & 1];
 #pragma unroll
     for (int j = 0; j < kPPT; ++j) {
       b0[j] = __ballot_sync(kFull, cat[j] & 1);
       b1[j] = __ballot_sync(kFull, cat[j] & 2);
-      if (lane == 0)
-        ws[j * NW + warp] = pack3(__popc(~(b0[j] | b1[j])), __popc(b0[j] & ~b1[j]), __popc(b1[j] & ~b0[j]));
+      if (lane == 0) wm[j * NW + warp] = make_uint2(b0[j], b1[j]);
     }
     __syncthreads();  // the only block barrier of a chunk
     // every thread holds its particles: refill this stage with chunk k+kStages
@@ -388,7 +387,11 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
     // prefixes are at most 32*(NE-1) < 1024 per field, so the packed sums
     // never carry between fields; the chunk totals come from the last entry
     // field by field.
-    const uint32_t v = lane < NE ? ws[lane] : 0u;
+    uint32_t v = 0u;  // lane e: the packed counts of entry e
+    if (lane < NE) {
+      const uint2 m = wm[lane];
+      v = pack3(__popc(~(m.x | m.y)), __popc(m.x & ~m.y), __popc(m.y & ~m.x));
+    }
     const uint32_t exl = __reduce_add_sync(kFull, lane < NE - 1 ? v : 0u);
     const uint32_t vl = __shfl_sync(kFull, v, NE - 1);
 #pragma unroll
