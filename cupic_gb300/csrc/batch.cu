@@ -41,7 +41,8 @@ struct cupic_batch {
   int *d_list = nullptr;
   int2 *d_rows = nullptr, *d_nodes = nullptr;
   unsigned *d_flags = nullptr;
-  float *d_res = nullptr, *d_halo = nullptr;
+  float *d_res = nullptr;
+  unsigned long long *d_halo = nullptr;  // halo words of all solves, zeroed at every build
   size_t cap_inst = 0, cap_groups = 0, cap_rows = 0, cap_nodes = 0, cap_flags = 0, cap_res = 0,
          cap_halo = 0;
   int ngroups = 0, nctas = 0, nrows = 0, nnodes = 0, max_nnx = 0, max_ncy = 0, max_inj = 0;
@@ -224,6 +225,8 @@ int build(cupic_batch *b) {
   if ((rc = grow(&b->d_flags, &b->cap_flags, nflags)) || (rc = grow(&b->d_res, &b->cap_res, nres)) ||
       (rc = grow(&b->d_halo, &b->cap_halo, nhalo)))
     return rc;
+  // a region may hold another instance's words with a matching epoch
+  CU(cudaMemsetAsync(b->d_halo, 0, sizeof(unsigned long long) * nhalo, b->stream));
   b->nflags = nflags;
   std::vector<JacobiArgs> jargs(n);
   size_t of = 0, orr = 0, oh = 0;

@@ -194,6 +194,8 @@ int alloc_jacobi_scratch(cupic_ctx *c, int G, long long GK, int P) {
   CU(dalloc(&c->jflags, (size_t)G + 1));
   CU(dalloc(&c->jres, (size_t)2 * G));
   CU(dalloc(&c->jhalo, (size_t)4 * GK * P));
+  // epoch 0 is never valid; the solves on the context's stream follow the clearing
+  CU(cudaMemsetAsync(c->jhalo, 0, sizeof(unsigned long long) * 4 * (size_t)GK * P, c->stream));
   return CUPIC_OK;
 }
 

@@ -29,7 +29,7 @@ struct cupic_ctx {
   bool jNoStrip = false;  // the tuner found the shared-memory sweep faster than register strips
   unsigned *jflags = nullptr;  // [G+1]: per-CTA sweep counters, then the barrier
   float *jres = nullptr;
-  float *jhalo = nullptr;
+  unsigned long long *jhalo = nullptr;  // halo words, zeroed at allocation
   // precision form of the solve (refine_every > 0): FP64 potential, FP32
   // residual source and correction, the residual's max norm
   double *phi64 = nullptr;

@@ -35,7 +35,9 @@ struct Ctl {
   unsigned long long absorbed[2];
   unsigned long long removed[2];
   int32_t abort;          // a bounded wait gave up: kernels bail out
-  int32_t pad;
+  uint32_t jepoch;        // solves run so far: the base of the halo words' epochs
+  uint32_t idle;          // never written: the bounded-wait self-test waits on it
+  uint32_t pad;
   cupic_step_stats ring[kStatsRing];
 };
 
@@ -92,7 +94,7 @@ struct JacobiArgs {
   unsigned int *flags;    // [G] last sweep published by each CTA
   unsigned int *bar;      // [1] grid barrier counter
   float *res_cta;         // [2*G] per-CTA max |dphi| of a checked sweep
-  float *halo;            // [2 parity][G][2 sides][depth rows][pitch]
+  unsigned long long *halo;  // [2 parity][G][2 sides][depth rows][pitch] {value, epoch} words
   float *phi;             // the potential solved for; NULL: a.phi
   const float *src;       // FP32 source per node; NULL: the charge accumulator a.rho[cur]
 };

@@ -5,12 +5,13 @@
 //
 // The potential stays resident in shared memory for the whole solve: CTA c
 // of a cooperative grid of G CTAs owns interior node rows [r0, r1) and keeps
-// them, one halo row on each side, in two shared buffers (true Jacobi, not
-// the reference's in-place update, defect D5).  After every sweep each CTA
-// publishes its first and last row to an L2-resident exchange buffer and
-// raises a per-CTA sweep counter; a CTA waits only for its two neighbours.
-// Convergence checks use a grid barrier, and every wait is bounded: when a
-// wait gives up the kernel raises CUPIC_FLAG_TIMEOUT and all CTAs return.
+// them, with K halo rows on each side, in two shared buffers (true Jacobi,
+// not the reference's in-place update, defect D5).  Every K sweeps each CTA
+// publishes its K first and K last rows to an L2-resident exchange buffer as
+// words tagged with the exchange's epoch; a CTA waits only for its two
+// neighbours' words.  Convergence checks use a grid barrier, and every wait
+// is bounded: when a wait gives up the kernel raises CUPIC_FLAG_TIMEOUT and
+// all CTAs return.
 #include <math.h>
 
 #include "cupic_internal.cuh"
@@ -22,6 +23,7 @@ namespace {
 
 constexpr int kJBlock = 512;
 constexpr long long kSpinLimit = 1ll << 22;
+constexpr int kHaloBatch = 4;  // halo rows per side polled together
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
   unsigned v;
@@ -29,8 +31,18 @@ __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
   return v;
 }
 
-__device__ __forceinline__ void st_release(unsigned *p, unsigned v) {
-  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+// Halo words: a value and the epoch of the exchange that wrote it in one
+// 64-bit word, written and read with single-copy-atomic relaxed accesses.
+// A reader that sees the epoch it waits for has the value, so an exchange
+// needs neither a fence nor a flag: one L2 round trip instead of three.
+__device__ __forceinline__ void st_word(unsigned long long *p, float v, unsigned ep) {
+  const unsigned long long w = ((unsigned long long)ep << 32) | __float_as_uint(v);
+  asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(w) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_word(const unsigned long long *p) {
+  unsigned long long w;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(w) : "l"(p) : "memory");
+  return w;
 }
 
 // spin until *p >= v; false if the wait gave up or another CTA aborted
@@ -174,12 +186,14 @@ template <int R, bool CHECK>
 __device__ __forceinline__ float sweep_reg(float4 (&x)[R], const float4 (&b)[R], const float *__restrict__ S,
                                            float *__restrict__ D, const RegGeom &g, int u0, int u1, int o0,
                                            int o1, bool full) {
+  // Straight-line code over the strip's rows: a row outside the strip or
+  // outside [u0, u1) computes from in-buffer addresses (row 0) and its
+  // result is discarded by selects and predicated stores, so the rows'
+  // independent chains can interleave.
   const int P = g.P, W = g.W, col = g.col;
-  float4 s4 = make_float4(0.f, 0.f, 0.f, 0.f), n4 = s4;
-  if (g.active && g.nvalid > 0) {
-    s4 = lds4(S + (g.lr0 - 1) * P + col);
-    n4 = lds4(S + (g.lr0 + g.nvalid) * P + col);
-  }
+  const bool any = g.active && g.nvalid > 0;
+  const float4 s4 = lds4(S + (any ? g.lr0 - 1 : 0) * P + col);
+  const float4 n4 = lds4(S + (any ? g.lr0 + g.nvalid : 0) * P + col);
   float4 prev = s4;
   float md = 0.0f;
 #pragma unroll
@@ -188,36 +202,31 @@ __device__ __forceinline__ float sweep_reg(float4 (&x)[R], const float4 (&b)[R],
     float lf = __shfl_up_sync(0xffffffffu, c.w, 1);
     float rt = __shfl_down_sync(0xffffffffu, c.x, 1);
     const int lr = g.lr0 + r;
-    if (g.active && r < g.nvalid) {
-      const float *rowp = S + lr * P;
-      if (g.lfix) lf = rowp[g.lcol];
-      if (g.rfix) rt = rowp[col + 4];
-      if (lr >= u0 && lr < u1) {
-        float4 nb = n4;
-        if (r + 1 < R && r + 1 < g.nvalid) nb = x[r + 1 < R ? r + 1 : r];
-        float4 v;
-        v.x = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].x, lf), c.y), nb.x), prev.x));
-        v.y = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].y, c.x), c.z), nb.y), prev.y));
-        v.z = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].z, c.y), c.w), nb.z), prev.z));
-        v.w = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].w, c.z), rt), nb.w), prev.w));
-        float *dp = D + lr * P;
-        if (full || r == 0 || r == g.nvalid - 1) {
-          *reinterpret_cast<float4 *>(dp + col) = v;
-        } else {
-          if (g.lfix) dp[col] = v.x;      // east neighbour of the lane before
-          if (g.rfix) dp[col + 3] = v.w;  // west neighbour of the lane after (or of column 0)
-        }
-        if (g.seam) dp[W] = v.x;
-        if (CHECK && lr >= o0 && lr < o1) {
-          md = fmaxf(md, fabsf(__fsub_rn(v.x, c.x)));
-          md = fmaxf(md, fabsf(__fsub_rn(v.y, c.y)));
-          md = fmaxf(md, fabsf(__fsub_rn(v.z, c.z)));
-          md = fmaxf(md, fabsf(__fsub_rn(v.w, c.w)));
-          if (g.seam) md = fmaxf(md, fabsf(__fsub_rn(v.x, rowp[W])));
-        }
-        x[r] = v;
-      }
+    const bool valid = g.active && r < g.nvalid;
+    const bool upd = valid && lr >= u0 && lr < u1;
+    const float *rowp = S + (valid ? lr : 0) * P;
+    if (g.lfix) lf = rowp[g.lcol];
+    if (g.rfix) rt = rowp[col + 4];
+    const float4 nb = (r + 1 < R && r + 1 < g.nvalid) ? x[r + 1 < R ? r + 1 : r] : n4;
+    float4 v;
+    v.x = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].x, lf), c.y), nb.x), prev.x));
+    v.y = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].y, c.x), c.z), nb.y), prev.y));
+    v.z = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].z, c.y), c.w), nb.z), prev.z));
+    v.w = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].w, c.z), rt), nb.w), prev.w));
+    float *dp = D + (valid ? lr : 0) * P;
+    const bool whole = full || r == 0 || r == g.nvalid - 1;
+    if (upd && whole) *reinterpret_cast<float4 *>(dp + col) = v;
+    if (upd && !whole && g.lfix) dp[col] = v.x;      // east neighbour of the lane before
+    if (upd && !whole && g.rfix) dp[col + 3] = v.w;  // west neighbour of the lane after (or of column 0)
+    if (upd && g.seam) dp[W] = v.x;
+    if (CHECK && upd && lr >= o0 && lr < o1) {
+      md = fmaxf(md, fabsf(__fsub_rn(v.x, c.x)));
+      md = fmaxf(md, fabsf(__fsub_rn(v.y, c.y)));
+      md = fmaxf(md, fabsf(__fsub_rn(v.z, c.z)));
+      md = fmaxf(md, fabsf(__fsub_rn(v.w, c.w)));
+      if (g.seam) md = fmaxf(md, fabsf(__fsub_rn(v.x, rowp[W])));
     }
+    x[r] = upd ? v : c;
     prev = c;  // the previous value of row r is the south neighbour of row r+1
   }
   return md;
@@ -252,6 +261,10 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
 
   float *const phi = J.phi ? J.phi : a.phi;
   const long long *acc = reinterpret_cast<const long long *>(a.rho[ctl->cur]);
+  // epochs of this solve's exchanges e = 1, 2, ...: (solve count << 16) + e,
+  // never 0 (the cleared buffer) and never those of an earlier solve's
+  // words still in the buffer
+  const unsigned ebase = *reinterpret_cast<volatile unsigned *>(&ctl->jepoch) << 16;
   for (int lr = 0; lr < nrows; ++lr) {
     const int j = lo + lr;
     const size_t rb = (size_t)j * nnx;
@@ -325,49 +338,65 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
                    : sweep_scalar<false>(S, D, bsrc, sg, u0, u1, o0, o1);
     }
   };
-  // Halo exchange.  The K rows of each side move as one batch per column
-  // block (all loads issued before the first store), so a transfer costs one
-  // L2 round trip rather than K.
+  // Halo exchange.  Each CTA writes its K first and K last rows as halo
+  // words of the exchange's epoch; the neighbours poll the words they need
+  // until every one carries that epoch.  The slots alternate by the
+  // exchange's parity: a CTA overwrites a slot two exchanges later, after
+  // its neighbours' next words, and so their reads of this one, arrived.
   auto publish = [&](const float *D, int e) {
-    float *hp = J.halo + ((size_t)(e & 1) * G + c) * 2 * K * P;
+    const unsigned ep = ebase + (unsigned)e;
+    unsigned long long *hp = J.halo + ((size_t)(e & 1) * G + c) * 2 * K * P;
     for (int i = tid; i < nnx; i += kJBlock) {
       for (int r = 0; r < K; ++r) {
-        __stcg(hp + r * P + i, D[(o0 + r) * P + i]);
-        __stcg(hp + (K + r) * P + i, D[(o1 - K + r) * P + i]);
+        st_word(hp + r * P + i, D[(o0 + r) * P + i], ep);
+        st_word(hp + (K + r) * P + i, D[(o1 - K + r) * P + i], ep);
       }
     }
-    __syncthreads();
-    if (tid == 0) st_release(&J.flags[c], (unsigned)e);
   };
   auto receive = [&](float *D, int e) -> bool {
-    if (tid == 0) {
-      bool ok = true;
-      if (c > 0) ok = wait_geq(&J.flags[c - 1], (unsigned)e, ctl);
-      if (ok && c < G - 1) ok = wait_geq(&J.flags[c + 1], (unsigned)e, ctl);
-      if (!ok) bail = 1;
+    const unsigned ep = ebase + (unsigned)e;
+    const unsigned long long *hlo = J.halo + ((size_t)(e & 1) * G + (c - 1)) * 2 * K * P + K * P;
+    const unsigned long long *hhi = J.halo + ((size_t)(e & 1) * G + (c + 1)) * 2 * K * P;
+    bool ok = true;
+    for (int i = tid; i < nnx && ok; i += kJBlock) {
+      for (int rb = 0; rb < K && ok; rb += kHaloBatch) {  // batches of rows per side, all loads in flight
+        unsigned long long wl[kHaloBatch], wh[kHaloBatch];
+        for (long long it = 0;; ++it) {
+          bool all = true;
+#pragma unroll
+          for (int q = 0; q < kHaloBatch; ++q) {
+            const int r = rb + q;
+            wl[q] = (r < K && c > 0) ? ld_word(hlo + r * P + i) : ((unsigned long long)ep << 32);
+            wh[q] = (r < K && c < G - 1) ? ld_word(hhi + r * P + i) : ((unsigned long long)ep << 32);
+          }
+#pragma unroll
+          for (int q = 0; q < kHaloBatch; ++q) all = all && (unsigned)(wl[q] >> 32) == ep && (unsigned)(wh[q] >> 32) == ep;
+          if (all) break;
+          if (it >= kSpinLimit || ((it & 255) == 255 && *(volatile int *)&ctl->abort)) {
+            ok = false;
+            break;
+          }
+          if (it > 4096) __nanosleep(32);
+        }
+        if (!ok) break;
+#pragma unroll
+        for (int q = 0; q < kHaloBatch; ++q) {
+          const int r = rb + q;
+          // the lower neighbour's last K rows, the upper neighbour's first K rows
+          if (r < K && c > 0) D[(o0 - K + r) * P + i] = __uint_as_float((unsigned)wl[q]);
+          if (r < K && c < G - 1) D[(o1 + r) * P + i] = __uint_as_float((unsigned)wh[q]);
+        }
+      }
+    }
+    if (!ok) {
+      if (!*(volatile int *)&ctl->abort) {
+        atomicExch(&ctl->abort, 1);
+        atomicOr(&ctl->step_flags, (uint32_t)CUPIC_FLAG_TIMEOUT);
+      }
+      bail = 1;
     }
     __syncthreads();
     if (bail) return false;
-    const float *hlo = J.halo + ((size_t)(e & 1) * G + (c - 1)) * 2 * K * P + K * P;
-    const float *hhi = J.halo + ((size_t)(e & 1) * G + (c + 1)) * 2 * K * P;
-    for (int i = tid; i < nnx; i += kJBlock) {
-      for (int rb = 0; rb < K; rb += 8) {  // batches of 8 rows: loads first, then stores
-        float vl[8], vh[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int r = rb + q;
-          vl[q] = (r < K && c > 0) ? __ldcg(hlo + r * P + i) : 0.0f;
-          vh[q] = (r < K && c < G - 1) ? __ldcg(hhi + r * P + i) : 0.0f;
-        }
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int r = rb + q;
-          if (r < K && c > 0) D[(o0 - K + r) * P + i] = vl[q];  // the lower neighbour's last K rows
-          if (r < K && c < G - 1) D[(o1 + r) * P + i] = vh[q];  // the upper neighbour's first K rows
-        }
-      }
-    }
-    __syncthreads();
     if constexpr (R > 0) {  // the strips' halo rows are new: reload their registers
 #pragma unroll
       for (int r = 0; r < R; ++r) {
@@ -485,6 +514,9 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
     ctl->sweeps = done;
     ctl->residual = last;
   }
+  // the next solve's epochs; every CTA read the base before its first
+  // exchange, which CTA 0's last receive depended on
+  if (c == 0 && tid == 0) ctl->jepoch = ctl->jepoch + 1u;
 }
 
 __device__ __forceinline__ void jacobi_dispatch(const SimArgs &a, const JacobiArgs &J, int c, float *jsm,
@@ -567,7 +599,7 @@ cudaError_t jacobi_max_ctas(size_t smem, int *per_sm) {
 // wait, on a word of the control block that nothing writes.  The wait gives
 // up after its iteration limit and raises CUPIC_FLAG_TIMEOUT.
 __global__ void k_wait_probe(SimArgs a) {
-  if (threadIdx.x == 0) wait_geq(reinterpret_cast<const unsigned *>(&a.ctl->pad), 1u, a.ctl);
+  if (threadIdx.x == 0) wait_geq(&a.ctl->idle, 1u, a.ctl);
 }
 
 cudaError_t launch_wait_probe(const SimArgs &a, cudaStream_t st) {

@@ -88,7 +88,7 @@ extern "C" int cupic_poisson_solver_static(const cupic_params *p, const int64_t 
   const long long rows_fit = (long long)(((size_t)dev_max - 1024) / (3 * sizeof(float) * (size_t)P));
   auto need = [&](int g, int k) {
     return kCtlHeadBytes + align256(sizeof(unsigned) * (size_t)(g + 1)) +
-           align256(sizeof(float) * 2 * (size_t)g) + sizeof(float) * (size_t)2 * g * 2 * k * P;
+           align256(sizeof(float) * 2 * (size_t)g) + sizeof(unsigned long long) * (size_t)2 * g * 2 * k * P;
   };
   // one CTA when the whole mesh fits; otherwise the most CTAs (up to one per
   // SM) for which some halo depth K >= 1 fits both the CTA's shared memory
@@ -127,7 +127,7 @@ extern "C" int cupic_poisson_solver_static(const cupic_params *p, const int64_t 
   q += align256(sizeof(unsigned) * (size_t)(G + 1));
   float *res = reinterpret_cast<float *>(q);
   q += align256(sizeof(float) * 2 * (size_t)G);
-  float *halo = reinterpret_cast<float *>(q);
+  unsigned long long *halo = reinterpret_cast<unsigned long long *>(q);
 
   unsigned long long *acc = reinterpret_cast<unsigned long long *>(const_cast<int64_t *>(rho_dev));
   a.rho[0] = acc;
@@ -156,8 +156,10 @@ extern "C" int cupic_poisson_solver_static(const cupic_params *p, const int64_t 
 
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   // the array keeps the previous call's contents: clear the status block
-  // (charge index 0, no abort, no flags); launch_jacobi clears the counters
-  if (cudaMemsetAsync(ctl, 0, kCtlHeadBytes, st) != cudaSuccess) return CUPIC_ERR_CUDA;
+  // (charge index 0, no abort, no flags) but not the epoch base, which
+  // keeps the halo words of earlier calls from matching; launch_jacobi
+  // clears the counters
+  if (cudaMemsetAsync(ctl, 0, offsetof(Ctl, jepoch), st) != cudaSuccess) return CUPIC_ERR_CUDA;
   if (launch_jacobi(a, J, st) != cudaSuccess) return CUPIC_ERR_CUDA;
   struct {
     uint32_t step_flags;
