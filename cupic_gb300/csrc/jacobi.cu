@@ -135,6 +135,67 @@ __device__ __forceinline__ float sweep_vec(const float *__restrict__ S, float *_
   return md;
 }
 
+// The same sweep with each thread walking up a column: thread (gx, gy)
+// computes the 4 nodes 4gx..4gx+3 of the consecutive rows [a0, a1), its
+// share of [u0, u1) split into RPI near-equal segments.  The rows below and
+// at the current one stay in registers from the previous step of the walk,
+// so a row costs two 16-byte loads (the row above and the source) instead
+// of four.  Every thread takes the same number of steps (the segment
+// length), so the shuffles always see all 32 lanes; steps past a thread's
+// segment compute from in-buffer rows and store nothing.
+template <bool CHECK>
+__device__ __forceinline__ float sweep_walk(const float *__restrict__ S, float *__restrict__ D,
+                                            const float *__restrict__ bsrc, const SweepGeom &g, int u0,
+                                            int u1, int o0, int o1) {
+  const int P = g.P, W = g.W;
+  const int n = u1 - u0;
+  const int seg = (n + g.RPI - 1) / g.RPI;
+  const int col = g.gx << 2;
+  const bool lfix = g.lane == 0 || g.gx == 0;
+  const bool rfix = g.lane == 31 || g.gx == g.TPR - 1;
+  const bool seam = g.gx == 0;
+  const int lcol = seam ? W - 1 : col - 1;
+  const bool active = g.gy < g.RPI;
+  const int a0 = u0 + (active ? g.gy : 0) * seg;
+  const int a1 = active ? min(u1, a0 + seg) : a0;
+  const int rs = a0 < u1 ? a0 : u0;  // first row read (in the buffer even for an empty segment)
+  float4 sv = *reinterpret_cast<const float4 *>(S + (rs - 1) * P + col);
+  float4 cv = *reinterpret_cast<const float4 *>(S + rs * P + col);
+  float md = 0.0f;
+  for (int t = 0; t < seg; ++t) {
+    const int lr = a0 + t;
+    const bool ok = lr < a1;
+    const int lrc = ok ? lr : rs;
+    const float *rowp = S + lrc * P;
+    const float4 nv = *reinterpret_cast<const float4 *>(rowp + P + col);
+    const float4 b4 = *reinterpret_cast<const float4 *>(bsrc + lrc * P + col);
+    float lf = __shfl_up_sync(0xffffffffu, cv.w, 1);
+    float rt = __shfl_down_sync(0xffffffffu, cv.x, 1);
+    if (ok) {
+      if (lfix) lf = rowp[lcol];
+      if (rfix) rt = rowp[col + 4];  // col+4 == W is the seam copy of node 0
+      float4 v;
+      v.x = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.x, lf), cv.y), nv.x), sv.x));
+      v.y = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.y, cv.x), cv.z), nv.y), sv.y));
+      v.z = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.z, cv.y), cv.w), nv.z), sv.z));
+      v.w = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b4.w, cv.z), rt), nv.w), sv.w));
+      float *dp = D + lr * P;
+      *reinterpret_cast<float4 *>(dp + col) = v;
+      if (seam) dp[W] = v.x;
+      if (CHECK && lr >= o0 && lr < o1) {
+        md = fmaxf(md, fabsf(__fsub_rn(v.x, cv.x)));
+        md = fmaxf(md, fabsf(__fsub_rn(v.y, cv.y)));
+        md = fmaxf(md, fabsf(__fsub_rn(v.z, cv.z)));
+        md = fmaxf(md, fabsf(__fsub_rn(v.w, cv.w)));
+        if (seam) md = fmaxf(md, fabsf(__fsub_rn(v.x, rowp[W])));
+      }
+    }
+    sv = cv;
+    cv = nv;
+  }
+  return md;
+}
+
 // the same sweep, one node per thread (used when (nnx-1) % 4 != 0)
 template <bool CHECK>
 __device__ __forceinline__ float sweep_scalar(const float *__restrict__ S, float *__restrict__ D,
@@ -239,7 +300,7 @@ __device__ __forceinline__ float sweep_reg(float4 (&x)[R], const float4 (&b)[R],
 // with the same operands as the neighbour, so the values are identical --
 // and the neighbours trade their k boundary rows only every k sweeps.
 // R > 0 selects the register-strip sweep with strips of R rows; R == 0 the
-// shared-memory sweep (sweep_vec / sweep_scalar).
+// shared-memory sweep (sweep_walk / sweep_vec / sweep_scalar).
 template <int R>
 __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &J, const int c, float *jsm,
                                             float *red, int *bail_p) {
@@ -332,6 +393,12 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
                    : sweep_reg<R, false>(x, bb, S, D, rg, u0, u1, o0, o1, full);
     } else {
       if (u0 >= u1) return 0.0f;
+      // long segments walk up the columns; short ones (a few rows per
+      // thread, where the walk's serial steps cost more than its loads
+      // save) take the rows in turn
+      if (vec && u1 - u0 >= 4 * sg.RPI)
+        return check ? sweep_walk<true>(S, D, bsrc, sg, u0, u1, o0, o1)
+                     : sweep_walk<false>(S, D, bsrc, sg, u0, u1, o0, o1);
       if (vec) return check ? sweep_vec<true>(S, D, bsrc, sg, u0, u1, o0, o1)
                             : sweep_vec<false>(S, D, bsrc, sg, u0, u1, o0, o1);
       return check ? sweep_scalar<true>(S, D, bsrc, sg, u0, u1, o0, o1)
