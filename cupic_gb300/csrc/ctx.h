@@ -36,6 +36,9 @@ struct cupic_ctx {
   float *rr = nullptr, *dl = nullptr;
   unsigned long long *maxr = nullptr;
   void *h_pin = nullptr;  // pinned: [0] max-norm bits, [1] {sweeps, residual}
+  // scratch of the host-format particle transfers, grown on demand and kept
+  void *io_buf = nullptr;
+  size_t io_cap = 0;
   // graph of one step
   cudaGraphExec_t graph = nullptr;
   bool graph_ok = false;
