@@ -10,7 +10,7 @@
 // Such a call still needs scratch memory for the solver CTAs: per-CTA sweep
 // counters, residual slots, the halo rows they trade, and a small status
 // block. Here that scratch is a file-scope static device array of a fixed
-// 4 MiB. Every GPU that loads this library holds it until the process
+// 8 MiB. Every GPU that loads this library holds it until the process
 // exits. The entry point rejects meshes whose scratch would not fit.
 #include <mutex>
 #include <stdlib.h>
@@ -24,7 +24,7 @@
 namespace cupic {
 namespace {
 
-constexpr size_t kStaticScratchBytes = size_t(4) << 20;
+constexpr size_t kStaticScratchBytes = size_t(8) << 20;
 constexpr size_t kCtlHeadBytes = 256;  // the part of Ctl the solver touches
 static_assert(offsetof(Ctl, ring) <= kCtlHeadBytes, "solver status block");
 

@@ -258,7 +258,7 @@ int cupic_test_bounded_wait(struct cupic_ctx *ctx);
  *   stream   a cudaStream_t, NULL for the default stream; the call waits for
  *            its own work before returning
  * The solver's scratch (sweep counters, residual slots and the halo rows its
- * CTAs trade) lives in a static 4 MiB device array that every GPU loading
+ * CTAs trade) lives in a static 8 MiB device array that every GPU loading
  * this library holds until exit.  The call lowers the halo depth, then the
  * CTA count, until the scratch fits; meshes for which nothing fits return
  * CUPIC_ERR_CAPACITY.  The largest ncy accepted is 5321 at ncx = 512, 2433

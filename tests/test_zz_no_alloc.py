@@ -84,7 +84,7 @@ def test_static_solve_matches_context_solver(gpu_lib, monkeypatch, name, over, c
 
 
 def test_static_solve_rejects_meshes_beyond_its_scratch(gpu_lib):
-    """A mesh whose exchange scratch exceeds the static 4 MiB is refused
+    """A mesh whose exchange scratch exceeds the static 8 MiB is refused
     before anything runs on the device."""
     torch = pytest.importorskip("torch")
     L = cg.load_library()
