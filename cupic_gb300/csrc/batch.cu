@@ -39,13 +39,13 @@ struct cupic_batch {
   JacobiArgs *d_jargs = nullptr;
   JGroup *d_groups = nullptr;
   int *d_list = nullptr;
-  int2 *d_rows = nullptr, *d_nodes = nullptr;
+  int2 *d_rows = nullptr;
   unsigned *d_flags = nullptr;
   float *d_res = nullptr;
   unsigned long long *d_halo = nullptr;  // halo words of all solves, zeroed at every build
-  size_t cap_inst = 0, cap_groups = 0, cap_rows = 0, cap_nodes = 0, cap_flags = 0, cap_res = 0,
+  size_t cap_inst = 0, cap_groups = 0, cap_rows = 0, cap_flags = 0, cap_res = 0,
          cap_halo = 0;
-  int ngroups = 0, nctas = 0, nrows = 0, nnodes = 0, max_nnx = 0, max_ncy = 0, max_inj = 0;
+  int ngroups = 0, nctas = 0, nrows = 0, max_nnx = 0, max_ncy = 0, max_inj = 0;
   // d_rows: rows of short-row instances (ncx <= kShortRow, pushed by
   // 256-thread blocks), then rows of mid-size ones (512-thread blocks),
   // then rows of big ones (ncy >= kBigRows), which are pushed by the
@@ -246,6 +246,7 @@ int build(cupic_batch *b) {
     J.strip = jacobi_strip_rows(c->a.nnx, q.B + 2 * (q.G > 1 ? q.K : 1) - 2);
     J.do_field = 1;
     J.write_stats = 1;
+    J.zero_next = 1;  // the solve clears the accumulator the push deposits into
     J.flags = b->d_flags + of;
     J.bar = J.flags + q.G;
     J.res_cta = b->d_res + orr;
@@ -256,7 +257,7 @@ int build(cupic_batch *b) {
     jargs[i] = J;
   }
   // work lists
-  std::vector<int2> rows, nodes;
+  std::vector<int2> rows;
   b->max_nnx_short = b->max_nnx_mid = 0;
   b->big.clear();
   auto cls = [&](int i) { return inst[i].ncy >= kBigRows ? 2 : inst[i].ncx <= kShortRow ? 0 : 1; };
@@ -273,14 +274,10 @@ int build(cupic_batch *b) {
     if (cls(r.x) == 0) ++b->nrows_short;
     if (cls(r.x) == 1) ++b->nrows_mid;
   }
-  for (int i = 0; i < n; ++i)
-    for (int j = 0; j < inst[i].nny; ++j) nodes.push_back(make_int2(i, j));
   b->nrows = (int)rows.size();
-  b->nnodes = (int)nodes.size();
   if ((rc = grow(&b->d_inst, &b->cap_inst, (size_t)n)) ||
       (rc = grow(&b->d_groups, &b->cap_groups, groups.size())) ||
-      (rc = grow(&b->d_rows, &b->cap_rows, rows.size())) ||
-      (rc = grow(&b->d_nodes, &b->cap_nodes, nodes.size())))
+      (rc = grow(&b->d_rows, &b->cap_rows, rows.size())))
     return rc;
   // d_jargs and d_list share the instance capacity
   static_assert(sizeof(JacobiArgs) >= sizeof(int), "");
@@ -295,7 +292,6 @@ int build(cupic_batch *b) {
   CU(cudaMemcpy(b->d_groups, groups.data(), groups.size() * sizeof(JGroup), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(b->d_list, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(b->d_rows, rows.data(), rows.size() * sizeof(int2), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(b->d_nodes, nodes.data(), nodes.size() * sizeof(int2), cudaMemcpyHostToDevice));
   return CUPIC_OK;
 }
 
@@ -309,7 +305,6 @@ int enqueue(cupic_batch *b) {
   CU(cudaStreamWaitEvent(b->side, b->ev_fork, 0));
   CU(launch_inject_draw_batch(b->d_inst, n, b->max_inj, b->side));
   CU(cudaEventRecord(b->ev_join, b->side));
-  CU(launch_zero_next_rho_batch(b->d_inst, b->d_nodes, b->nnodes, st));
   // big instances: the single-context push, one launch each, on parallel
   // branches beside the work-list pushes of the others
   const int nbr = b->big.empty() ? 0 : std::min(kPushBranches, (int)b->big.size());
@@ -442,7 +437,6 @@ int cupic_batch_destroy(cupic_batch *b) {
   cudaFree(b->d_groups);
   cudaFree(b->d_list);
   cudaFree(b->d_rows);
-  cudaFree(b->d_nodes);
   cudaFree(b->d_flags);
   cudaFree(b->d_res);
   cudaFree(b->d_halo);

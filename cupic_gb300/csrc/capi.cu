@@ -479,6 +479,19 @@ int run_solve(cupic_ctx *c, double tol, int mn, int mx, int chk, int field, int 
   return CUPIC_OK;
 }
 
+// a step's solve, which also clears the next charge accumulator (the
+// precision form's solve does not: the step clears it separately)
+int run_step_solve(cupic_ctx *c, bool *zeroed) {
+  const cupic_params &p = c->p;
+  *zeroed = false;
+  if (p.refine_every > 0) return refine_solve(c, p.tol, p.min_sweeps, p.max_sweeps, 1, 1);
+  JacobiArgs J = jargs(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1);
+  J.zero_next = 1;
+  CU(launch_jacobi(c->a, J, c->stream));
+  *zeroed = true;
+  return CUPIC_OK;
+}
+
 int deposit_current(cupic_ctx *c) {
   CU(cudaMemsetAsync(c->a.rho[c->host_cur], 0,
                      sizeof(unsigned long long) * (size_t)c->a.nnx * c->a.nny, c->stream));
@@ -521,12 +534,12 @@ int finish(cupic_ctx *c) {
 // One step: solve + field, then the injection draws on the side stream while
 // the main stream clears the next charge, pushes and appends the movers;
 // the injected particles are appended once both branches are done.
-int enqueue_after_solve(cupic_ctx *c) {
+int enqueue_after_solve(cupic_ctx *c, bool zeroed) {
   CU(cudaEventRecord(c->ev_fork, c->stream));
   CU(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
   CU(launch_inject_draw(c->a, c->side));
   CU(cudaEventRecord(c->ev_join, c->side));
-  CU(launch_zero_next_rho(c->a, c->stream));
+  if (!zeroed) CU(launch_zero_next_rho(c->a, c->stream));
   CU(launch_push_deposit(c->a, c->stream));
   CU(launch_arrive(c->a, c->stream));
   CU(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
@@ -536,10 +549,10 @@ int enqueue_after_solve(cupic_ctx *c) {
 }
 
 int enqueue_step(cupic_ctx *c) {
-  const cupic_params &p = c->p;
-  int rc = run_solve(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1);
+  bool zeroed = false;
+  int rc = run_step_solve(c, &zeroed);
   if (rc) return rc;
-  return enqueue_after_solve(c);
+  return enqueue_after_solve(c, zeroed);
 }
 
 int capture_step(cupic_ctx *c) {
@@ -1125,7 +1138,8 @@ int cupic_step_timed(cupic_ctx *c, int32_t nsteps, float *phase_ms, int32_t npha
   for (auto &e : ev)
     if (cudaEventCreate(&e) != cudaSuccess) rc = CUPIC_ERR_CUDA;
   const cupic_params &p = c->p;
-  const JacobiArgs J = jargs(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1);
+  JacobiArgs J = jargs(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1);
+  J.zero_next = 1;  // as in a step: the solve clears the next charge accumulator
   cudaError_t e = rc ? cudaErrorUnknown : cudaEventRecord(ev[0], c->stream);
   for (int s = 0; s < nsteps && e == cudaSuccess; ++s) {
     // the launch order of enqueue_step, with an event after each
@@ -1144,7 +1158,7 @@ int cupic_step_timed(cupic_ctx *c, int32_t nsteps, float *phase_ms, int32_t npha
     if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
     if (e == cudaSuccess) e = launch_inject_draw(c->a, c->side);
     if (e == cudaSuccess) e = cudaEventRecord(c->ev_join, c->side);
-    if (e == cudaSuccess) e = launch_zero_next_rho(c->a, c->stream);
+    if (e == cudaSuccess && c->p.refine_every > 0) e = launch_zero_next_rho(c->a, c->stream);
     if (e == cudaSuccess) e = cudaEventRecord(q[1], c->stream);
     if (e == cudaSuccess) e = launch_push_deposit(c->a, c->stream);
     if (e == cudaSuccess) e = cudaEventRecord(q[2], c->stream);

@@ -91,6 +91,7 @@ struct JacobiArgs {
   int32_t strip;          // 0: shared-memory sweep; 1, 2, 4, 8: rows kept in registers per thread
   int32_t do_field;       // 1: derive E after the last sweep
   int32_t write_stats;    // 1: store sweeps/residual in the control block
+  int32_t zero_next;      // 1: also clear the next charge accumulator a.rho[cur^1] (a step's solve)
   unsigned int *flags;    // [G] last sweep published by each CTA
   unsigned int *bar;      // [1] grid barrier counter
   float *res_cta;         // [2*G] per-CTA max |dphi| of a checked sweep

@@ -326,6 +326,13 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
   // never 0 (the cleared buffer) and never those of an earlier solve's
   // words still in the buffer
   const unsigned ebase = *reinterpret_cast<volatile unsigned *>(&ctl->jepoch) << 16;
+  if (J.zero_next) {
+    // the accumulator the step's push deposits into: this CTA's rows, and
+    // the boundary rows from the first and last CTA
+    unsigned long long *nx = a.rho[ctl->cur ^ 1];
+    const int z0 = c == 0 ? 0 : r0, z1 = c == G - 1 ? nny : r1;
+    for (size_t k = (size_t)z0 * nnx + tid; k < (size_t)z1 * nnx; k += kJBlock) nx[k] = 0ull;
+  }
   for (int lr = 0; lr < nrows; ++lr) {
     const int j = lo + lr;
     const size_t rb = (size_t)j * nnx;

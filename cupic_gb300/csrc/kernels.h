@@ -43,8 +43,6 @@ cudaError_t jacobi_batch_set_smem(size_t bytes);
 cudaError_t jacobi_batch_max_ctas(size_t smem, int *per_sm);
 cudaError_t launch_jacobi_batch(const SimArgs *inst, const JacobiArgs *jargs, const JGroup *groups,
                                 int ngroups, const int *list, int nctas, size_t smem, cudaStream_t st);
-cudaError_t launch_zero_next_rho_batch(const SimArgs *inst, const int2 *node_work, int n,
-                                       cudaStream_t st);
 cudaError_t launch_push_deposit_batch(const SimArgs *inst, const int2 *row_work, int n, int max_nnx,
                                       int threads, cudaStream_t st);
 cudaError_t launch_arrive_batch(const SimArgs *inst, const int2 *row_work, int n, cudaStream_t st);

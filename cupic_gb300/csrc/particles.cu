@@ -674,47 +674,66 @@ __device__ __forceinline__ void finalize(const SimArgs &a) {
   __shared__ unsigned long long live[2];
   if (threadIdx.x < 2) live[threadIdx.x] = 0ull;
   __syncthreads();
-  for (int sp = 0; sp < 2; ++sp) {
-    unsigned long long v = 0;
-    for (int k = threadIdx.x; k < a.ncy; k += blockDim.x) v += (unsigned long long)a.sp[sp].cnt[k];
-    atomicAdd(&live[sp], v);
+  // both species' counts in one loop, so each thread's loads of a pass
+  // are in flight together
+  unsigned long long v0 = 0, v1 = 0;
+  for (int k = threadIdx.x; k < a.ncy; k += blockDim.x) {
+    v0 += (unsigned long long)a.sp[0].cnt[k];
+    v1 += (unsigned long long)a.sp[1].cnt[k];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    v0 += __shfl_down_sync(0xffffffffu, v0, o);
+    v1 += __shfl_down_sync(0xffffffffu, v1, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&live[0], v0);
+    atomicAdd(&live[1], v1);
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    cupic_step_stats &st = ctl->ring[ctl->step % kStatsRing];
-    st.step = ctl->step;
-    st.t = ctl->t;
+    // every field is read before the first store: the ring entry lies in
+    // the same block, so interleaved loads and stores would each wait for
+    // the one before (one L2 round trip per field)
+    const int64_t step = ctl->step;
+    const double t = ctl->t;
+    const unsigned long long ab0 = ctl->absorbed[0], ab1 = ctl->absorbed[1];
+    const unsigned long long rm0 = ctl->removed[0], rm1 = ctl->removed[1];
+    const int32_t in0 = ctl->inj_count[0], in1 = ctl->inj_count[1];
+    const int32_t sweeps = ctl->sweeps;
+    const float residual = ctl->residual;
+    const uint32_t sfl = ctl->step_flags, fl = ctl->flags;
+    const int32_t cur = ctl->cur;
+    cupic_step_stats st{};
+    st.step = step;
+    st.t = t;
+    st.absorbed[0] = (int64_t)ab0;
+    st.absorbed[1] = (int64_t)ab1;
+    st.removed[0] = (int64_t)rm0;
+    st.removed[1] = (int64_t)rm1;
+    st.injected[0] = in0;
+    st.injected[1] = in1;
+    st.live[0] = (int64_t)live[0];
+    st.live[1] = (int64_t)live[1];
+    st.sweeps = sweeps;
+    st.residual = residual;
+    st.flags = sfl;
+    ctl->ring[step % kStatsRing] = st;
     for (int sp = 0; sp < 2; ++sp) {
-      st.absorbed[sp] = (int64_t)ctl->absorbed[sp];
-      st.removed[sp] = (int64_t)ctl->removed[sp];
-      st.injected[sp] = ctl->inj_count[sp];
-      st.live[sp] = (int64_t)live[sp];
       ctl->absorbed[sp] = 0ull;
       ctl->removed[sp] = 0ull;
       ctl->inj_count[sp] = 0;
     }
-    st.sweeps = ctl->sweeps;
-    st.residual = ctl->residual;
-    st.flags = ctl->step_flags;
-    ctl->flags |= ctl->step_flags;
+    ctl->flags = fl | sfl;
     ctl->step_flags = 0u;
-    ctl->t = ctl->t + a.dt_d;
-    ctl->step = ctl->step + 1;
-    ctl->cur ^= 1;
+    ctl->t = t + a.dt_d;
+    ctl->step = step + 1;
+    ctl->cur = cur ^ 1;
   }
 }
 
 __global__ void k_finalize(SimArgs a) { finalize(a); }
 
 __global__ void k_finalize_batch(const SimArgs *__restrict__ inst) { finalize(inst[blockIdx.x]); }
-
-// work[b] = {instance, node row}
-__global__ void k_zero_next_rho_batch(const SimArgs *__restrict__ inst, const int2 *__restrict__ work) {
-  const int2 w = work[blockIdx.x];
-  const SimArgs &a = inst[w.x];
-  unsigned long long *r = a.rho[a.ctl->cur ^ 1] + (size_t)w.y * a.nnx;
-  for (int i = threadIdx.x; i < a.nnx; i += blockDim.x) r[i] = 0ull;
-}
 
 // ---------------------------------------------------------------------------
 // launch helpers
@@ -785,12 +804,6 @@ cudaError_t launch_inject(const SimArgs &a, cudaStream_t st) {
   return launch_inject_append(a, st);
 }
 
-cudaError_t launch_zero_next_rho_batch(const SimArgs *inst, const int2 *node_work, int n,
-                                       cudaStream_t st) {
-  k_zero_next_rho_batch<<<n, 256, 0, st>>>(inst, node_work);
-  return cudaGetLastError();
-}
-
 template <int PB>
 cudaError_t push_batch(const SimArgs *inst, const int2 *row_work, int n, int max_nnx, cudaStream_t st) {
   static size_t cur = 48 * 1024;  // the attribute only grows
@@ -836,7 +849,7 @@ cudaError_t launch_finalize_batch(const SimArgs *inst, int n, cudaStream_t st) {
 }
 
 cudaError_t launch_finalize(const SimArgs &a, cudaStream_t st) {
-  k_finalize<<<1, 256, 0, st>>>(a);
+  k_finalize<<<1, 1024, 0, st>>>(a);
   return cudaGetLastError();
 }
 
