@@ -252,7 +252,13 @@ struct CicFixed {
   int ic, jc;
   int FX, FY;  // offsets in the cell, 16 fractional bits, in [0, 65536]
   int FXY;     // round(FX*FY / 2^16), in [0, 65536]
-  long long w00, w10, w01, w11;
+  // the four node weights, formed where needed
+  __device__ __forceinline__ long long w11() const { return (long long)FXY << 16; }
+  __device__ __forceinline__ long long w10() const { return ((long long)FX << 16) - w11(); }
+  __device__ __forceinline__ long long w01() const { return ((long long)FY << 16) - w11(); }
+  __device__ __forceinline__ long long w00() const {
+    return 4294967296ll - (((long long)FX + FY) << 16) + w11();
+  }
 };
 
 // INSIDE: the caller knows 0 <= x < Lx and 0 <= y < Ly.  Then the cell
@@ -277,11 +283,6 @@ __device__ __forceinline__ CicFixed cic_fixed(const SimArgs &a, float x, float y
   r.FX = __float2int_rn(f.x);
   r.FY = __float2int_rn(f.y);
   r.FXY = (int)(((unsigned long long)r.FX * (unsigned long long)r.FY + 32768ull) >> 16);
-  const long long FX = r.FX, FY = r.FY, W11 = (long long)r.FXY << 16;
-  r.w11 = W11;
-  r.w10 = (FX << 16) - W11;
-  r.w01 = (FY << 16) - W11;
-  r.w00 = 4294967296ll - ((FX + FY) << 16) + W11;
   return r;
 }
 

@@ -66,10 +66,10 @@ struct RhoMoments {
       atomicAdd(mc + 3, (unsigned)c.FXY);
     } else {
       const size_t n00 = (size_t)c.jc * nnx + c.ic;
-      atomicAdd(&g[n00], (unsigned long long)(q * c.w00));
-      atomicAdd(&g[n00 + 1], (unsigned long long)(q * c.w10));
-      atomicAdd(&g[n00 + nnx], (unsigned long long)(q * c.w01));
-      atomicAdd(&g[n00 + nnx + 1], (unsigned long long)(q * c.w11));
+      atomicAdd(&g[n00], (unsigned long long)(q * c.w00()));
+      atomicAdd(&g[n00 + 1], (unsigned long long)(q * c.w10()));
+      atomicAdd(&g[n00 + nnx], (unsigned long long)(q * c.w01()));
+      atomicAdd(&g[n00 + nnx + 1], (unsigned long long)(q * c.w11()));
     }
   }
   __device__ __forceinline__ void zero() const {
@@ -635,11 +635,11 @@ __device__ __forceinline__ void inject_append(const SimArgs &a, const int sp, in
       if (pos < S.cap[d]) {
         S.parts[S.seg[d] + pos] = p;
         const CicFixed c = cic_fixed(a, p.x, p.y);
-        atomicAdd(&rho_next[(size_t)c.jc * a.nnx + c.ic], (unsigned long long)(q * c.w00));
-        atomicAdd(&rho_next[(size_t)c.jc * a.nnx + c.ic + 1], (unsigned long long)(q * c.w10));
-        atomicAdd(&rho_next[(size_t)(c.jc + 1) * a.nnx + c.ic], (unsigned long long)(q * c.w01));
+        atomicAdd(&rho_next[(size_t)c.jc * a.nnx + c.ic], (unsigned long long)(q * c.w00()));
+        atomicAdd(&rho_next[(size_t)c.jc * a.nnx + c.ic + 1], (unsigned long long)(q * c.w10()));
+        atomicAdd(&rho_next[(size_t)(c.jc + 1) * a.nnx + c.ic], (unsigned long long)(q * c.w01()));
         atomicAdd(&rho_next[(size_t)(c.jc + 1) * a.nnx + c.ic + 1],
-                  (unsigned long long)(q * c.w11));
+                  (unsigned long long)(q * c.w11()));
       } else {
         fl |= CUPIC_FLAG_CAPACITY;
       }
