@@ -37,33 +37,34 @@ __device__ __forceinline__ void raise_flags(Ctl *ctl, uint32_t f) {
 // Over the particles of a cell the four node sums follow from four integer
 // moments M1 = count, MX = sum FX, MY = sum FY, MXY = sum FXY by the same
 // formulas.  Shared memory atomics are native for 32-bit integers only, so
-// a particle adds 1, FX, FY and FXY to the four unsigned moments of its cell
-// (stored together at an odd stride, one address per particle).  The moments of one species
-// over at most kFoldParticles particles stay below 2^32; fold(q) turns them
-// into int64 node sums times the species charge q, added to global memory,
-// that often and at every change of species.  Deposits whose cell row is
-// outside the tile go straight to global memory as int64 node weights.
+// a particle adds 1, FX, FY and FXY to the four unsigned moments of its
+// cell, held in four arrays (one per moment): the lanes of a warp, on
+// cells spread over the row, spread over the banks.  The moments of one
+// species over at most kFoldParticles particles stay below 2^32; fold(q)
+// turns them into int64 node sums times the species charge q, added to
+// global memory, that often and at every change of species.  Deposits
+// whose cell row is outside the tile go straight to global memory as int64
+// node weights.
 constexpr int kFoldParticles = 63 * 1024;  // 64512 * 65536 < 2^32
-// words per cell: odd, so that lanes depositing to different cells of a
-// row hit different shared-memory banks
-constexpr int kMomStride = 5;
 
 struct RhoMoments {
-  unsigned *m;     // [ncr*ncx][kMomStride]: M1, MX, MY, MXY (and one unused word)
+  unsigned *m;     // [4][ncr*ncx]: M1, MX, MY, MXY
   int crow0, ncr, ncx, nnx, nny;
   unsigned long long *g;
 
+  __device__ __forceinline__ int cells() const { return ncr * ncx; }
   __device__ __forceinline__ void deposit(const SimArgs &a, float x, float y, int q) const {
     deposit(cic_fixed(a, x, y), q);
   }
   __device__ __forceinline__ void deposit(const CicFixed &c, int q) const {
     const int tr = c.jc - crow0;
     if (tr >= 0 && tr < ncr) {
-      unsigned *mc = m + kMomStride * (tr * ncx + c.ic);
+      const int nc = cells();
+      unsigned *mc = m + (tr * ncx + c.ic);
       atomicAdd(mc, 1u);
-      atomicAdd(mc + 1, (unsigned)c.FX);
-      atomicAdd(mc + 2, (unsigned)c.FY);
-      atomicAdd(mc + 3, (unsigned)c.FXY);
+      atomicAdd(mc + nc, (unsigned)c.FX);
+      atomicAdd(mc + 2 * nc, (unsigned)c.FY);
+      atomicAdd(mc + 3 * nc, (unsigned)c.FXY);
     } else {
       const size_t n00 = (size_t)c.jc * nnx + c.ic;
       atomicAdd(&g[n00], (unsigned long long)(q * c.w00()));
@@ -73,11 +74,12 @@ struct RhoMoments {
     }
   }
   __device__ __forceinline__ void zero() const {
-    for (int k = threadIdx.x; k < kMomStride * ncr * ncx; k += blockDim.x) m[k] = 0u;
+    for (int k = threadIdx.x; k < 4 * cells(); k += blockDim.x) m[k] = 0u;
   }
-  __device__ __forceinline__ long long mxy(int c) const {
-    return (long long)m[kMomStride * c + 3] << 16;
-  }
+  __device__ __forceinline__ long long m1(int c) const { return (long long)m[c]; }
+  __device__ __forceinline__ long long mx(int c) const { return (long long)m[cells() + c]; }
+  __device__ __forceinline__ long long my(int c) const { return (long long)m[2 * cells() + c]; }
+  __device__ __forceinline__ long long mxy(int c) const { return (long long)m[3 * cells() + c] << 16; }
   // moments (of charge q particles) -> node sums added to global memory,
   // then clear the moments; callers __syncthreads() before, and before the
   // next deposit
@@ -87,16 +89,15 @@ struct RhoMoments {
       long long v = 0;
       if (i < ncx && j < ncr) {  // this node is the lower-left corner of cell (i, j)
         const int c = j * ncx + i;
-        v += (long long)m[kMomStride * c] * 4294967296ll -
-             65536ll * ((long long)m[kMomStride * c + 1] + (long long)m[kMomStride * c + 2]) + mxy(c);
+        v += m1(c) * 4294967296ll - 65536ll * (mx(c) + my(c)) + mxy(c);
       }
       if (i >= 1 && j < ncr) {  // lower-right corner of cell (i-1, j)
         const int c = j * ncx + i - 1;
-        v += 65536ll * (long long)m[kMomStride * c + 1] - mxy(c);
+        v += 65536ll * mx(c) - mxy(c);
       }
       if (i < ncx && j >= 1) {  // upper-left corner of cell (i, j-1)
         const int c = (j - 1) * ncx + i;
-        v += 65536ll * (long long)m[kMomStride * c + 2] - mxy(c);
+        v += 65536ll * my(c) - mxy(c);
       }
       if (i >= 1 && j >= 1) {  // upper-right corner of cell (i-1, j-1)
         v += mxy((j - 1) * ncx + i - 1);
@@ -106,12 +107,12 @@ struct RhoMoments {
         atomicAdd(&g[(size_t)r * nnx + i], (unsigned long long)(q * v));
     }
     __syncthreads();
-    for (int k = threadIdx.x; k < kMomStride * ncr * ncx; k += blockDim.x) m[k] = 0u;
+    for (int k = threadIdx.x; k < 4 * cells(); k += blockDim.x) m[k] = 0u;
   }
 };
 
 __host__ __device__ constexpr size_t rho_moment_bytes(int ncr, int ncx) {
-  return (size_t)5 * ncr * ncx * sizeof(unsigned);
+  return (size_t)4 * ncr * ncx * sizeof(unsigned);
 }
 
 // classification of a pushed particle listed in row s (s < 0: injected)
