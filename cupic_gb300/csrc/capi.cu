@@ -470,9 +470,46 @@ int refine_solve(cupic_ctx *c, double tol, int mn, int mx, int field, int write_
   return CUPIC_OK;
 }
 
+// The same solve with the stop test on the device: every correction of the
+// sweep cap is enqueued (residual, test, m sweeps, update), and once the
+// test has passed the remaining kernels return at once.  Nothing waits on
+// the host, so a step in the precision form is captured as one graph.  The
+// kernels, their order and their operands are those of refine_solve, so
+// the results are identical.  Caps needing more than kDeviceCorrections
+// corrections use refine_solve.
+constexpr int kDeviceCorrections = 512;
+
+bool refine_on_device(const cupic_ctx *c, int mx) {
+  const int m = c->p.refine_every;
+  return (long long)(std::max(mx, 0) + m - 1) / m <= kDeviceCorrections;
+}
+
+int refine_solve_device(cupic_ctx *c, double tol, int mn, int mx, int field, int write_stats) {
+  const int m = c->p.refine_every;
+  CU(cudaMemsetAsync(&c->ctl->refine_done, 0, sizeof(int32_t), c->stream));
+  for (int sweeps = 0;;) {
+    CU(launch_r64_residual(c->a, c->phi64, c->rr, c->dl, c->maxr, c->stream, 1));
+    CU(launch_r64_decide(c->a, c->maxr, sweeps, mn, mx, tol, write_stats, c->stream));
+    if (sweeps >= mx) break;
+    const int k = std::min(m, mx - sweeps);
+    JacobiArgs J = jargs(c, 0.0, k, k, k, 0);
+    J.write_stats = 0;
+    J.phi = c->dl;
+    J.src = c->rr;
+    J.gated = 1;
+    CU(launch_jacobi(c->a, J, c->stream));
+    CU(launch_r64_update(c->a, c->phi64, c->dl, c->stream, 1));
+    sweeps += k;
+  }
+  if (field) CU(launch_r64_field(c->a, c->phi64, c->stream));
+  return CUPIC_OK;
+}
+
 // the solve of a step or stage call, FP32 or in the precision form
 int run_solve(cupic_ctx *c, double tol, int mn, int mx, int chk, int field, int write_stats = 1) {
-  if (c->p.refine_every > 0) return refine_solve(c, tol, mn, mx, field, write_stats);
+  if (c->p.refine_every > 0)
+    return refine_on_device(c, mx) ? refine_solve_device(c, tol, mn, mx, field, write_stats)
+                                   : refine_solve(c, tol, mn, mx, field, write_stats);
   JacobiArgs J = jargs(c, tol, mn, mx, chk, field);
   J.write_stats = write_stats;
   CU(launch_jacobi(c->a, J, c->stream));
@@ -484,7 +521,7 @@ int run_solve(cupic_ctx *c, double tol, int mn, int mx, int chk, int field, int 
 int run_step_solve(cupic_ctx *c, bool *zeroed) {
   const cupic_params &p = c->p;
   *zeroed = false;
-  if (p.refine_every > 0) return refine_solve(c, p.tol, p.min_sweeps, p.max_sweeps, 1, 1);
+  if (p.refine_every > 0) return run_solve(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1);
   JacobiArgs J = jargs(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1);
   J.zero_next = 1;
   CU(launch_jacobi(c->a, J, c->stream));
@@ -1057,7 +1094,8 @@ int cupic_step(cupic_ctx *c, int32_t nsteps) {
     int rc = deposit_current(c);
     if (rc) return rc;
   }
-  if (c->p.refine_every > 0) {  // the solve reads its residual norm on the host: no graph
+  if (c->p.refine_every > 0 && !refine_on_device(c, c->p.max_sweeps)) {
+    // the solve reads its residual norm on the host: no graph
     for (int i = 0; i < nsteps; ++i) {
       int rc = enqueue_step(c);
       if (rc) return rc;
@@ -1147,7 +1185,7 @@ int cupic_step_timed(cupic_ctx *c, int32_t nsteps, float *phase_ms, int32_t npha
     // (draws) plus the append
     cudaEvent_t *q = &ev[(size_t)s * per + 1];
     if (c->p.refine_every > 0) {
-      const int r = refine_solve(c, p.tol, p.min_sweeps, p.max_sweeps, 1, 1);
+      const int r = run_solve(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1);
       if (r) rc = r;
       e = r ? cudaErrorUnknown : cudaSuccess;
     } else {

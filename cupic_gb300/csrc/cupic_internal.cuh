@@ -37,7 +37,7 @@ struct Ctl {
   int32_t abort;          // a bounded wait gave up: kernels bail out
   uint32_t jepoch;        // solves run so far: the base of the halo words' epochs
   uint32_t idle;          // never written: the bounded-wait self-test waits on it
-  uint32_t pad;
+  int32_t refine_done;    // precision-form solve: the stop test passed, later corrections idle
   cupic_step_stats ring[kStatsRing];
 };
 
@@ -92,6 +92,7 @@ struct JacobiArgs {
   int32_t do_field;       // 1: derive E after the last sweep
   int32_t write_stats;    // 1: store sweeps/residual in the control block
   int32_t zero_next;      // 1: also clear the next charge accumulator a.rho[cur^1] (a step's solve)
+  int32_t gated;          // 1: return at once when ctl->refine_done is set (precision-form correction)
   unsigned int *flags;    // [G] last sweep published by each CTA
   unsigned int *bar;      // [1] grid barrier counter
   float *res_cta;         // [2*G] per-CTA max |dphi| of a checked sweep

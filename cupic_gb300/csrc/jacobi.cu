@@ -24,6 +24,7 @@ namespace {
 constexpr int kJBlock = 512;
 constexpr long long kSpinLimit = 1ll << 22;
 constexpr int kHaloBatch = 4;  // halo rows per side polled together
+constexpr int kLoadBatch = 8;  // mesh values per thread loaded together at the start
 
 __device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
   unsigned v;
@@ -305,6 +306,7 @@ template <int R>
 __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &J, const int c, float *jsm,
                                             float *red, int *bail_p) {
   int &bail = *bail_p;
+  if (J.gated && *reinterpret_cast<volatile int *>(&a.ctl->refine_done)) return;  // uniform: a flag of an earlier kernel
   const int G = J.G, tid = threadIdx.x;
   const int nnx = a.nnx, nny = a.nny, P = J.pitch;
   const int M = nny - 2;
@@ -333,20 +335,40 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
     const int z0 = c == 0 ? 0 : r0, z1 = c == G - 1 ? nny : r1;
     for (size_t k = (size_t)z0 * nnx + tid; k < (size_t)z1 * nnx; k += kJBlock) nx[k] = 0ull;
   }
-  for (int lr = 0; lr < nrows; ++lr) {
-    const int j = lo + lr;
-    const size_t rb = (size_t)j * nnx;
-    const bool interior = j >= 1 && j <= nny - 2;
-    for (int i = tid; i < nnx; i += kJBlock) {
-      const float v = phi[rb + i];
-      buf0[lr * P + i] = v;
-      buf1[lr * P + i] = v;
-      if (interior) {
-        if (J.src) {
-          bsrc[lr * P + i] = J.src[rb + i];
-        } else {
-          const long long f = (i == 0 || i == nnx - 1) ? acc[rb] + acc[rb + nnx - 1] : acc[rb + i];
-          bsrc[lr * P + i] = __double2float_rn((double)f * a.cb);
+  // Load the buffered rows: the (row, column) pairs taken kLoadBatch at a
+  // time per thread with all their loads issued before the first store, so
+  // a batch costs one memory round trip instead of one per row.
+  {
+    const int total = nrows * nnx;
+    for (int k0 = tid; k0 < total; k0 += kJBlock * kLoadBatch) {
+      float v[kLoadBatch], bv[kLoadBatch];
+#pragma unroll
+      for (int u = 0; u < kLoadBatch; ++u) {
+        const int k = k0 + u * kJBlock;
+        v[u] = 0.0f;
+        bv[u] = 0.0f;
+        if (k < total) {
+          const int lr = k / nnx, i = k - lr * nnx, j = lo + lr;
+          const size_t rb = (size_t)j * nnx;
+          v[u] = phi[rb + i];
+          if (j >= 1 && j <= nny - 2) {
+            if (J.src) {
+              bv[u] = J.src[rb + i];
+            } else {
+              const long long f = (i == 0 || i == nnx - 1) ? acc[rb] + acc[rb + nnx - 1] : acc[rb + i];
+              bv[u] = __double2float_rn((double)f * a.cb);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < kLoadBatch; ++u) {
+        const int k = k0 + u * kJBlock;
+        if (k < total) {
+          const int lr = k / nnx, i = k - lr * nnx, j = lo + lr;
+          buf0[lr * P + i] = v[u];
+          buf1[lr * P + i] = v[u];
+          if (j >= 1 && j <= nny - 2) bsrc[lr * P + i] = bv[u];
         }
       }
     }
@@ -486,7 +508,9 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
   for (int s = 1; s <= J.max_sweeps; ++s) {
     float *S = src ? buf1 : buf0;
     float *D = src ? buf0 : buf1;
-    const bool check = (--to_check == 0) || (s == J.max_sweeps);
+    // a solve with no tolerance that reports nothing (a correction of the
+    // precision form) needs no residual: no check, no grid barrier
+    const bool check = ((--to_check == 0) || (s == J.max_sweeps)) && (J.tol > 0.0 || J.write_stats);
     if (to_check == 0) to_check = J.check_every;
     m = (m >= K) ? 1 : m + 1;                        // position in the temporal block
     const int u0 = max(1, r0 - K + m) - lo;          // updated local rows [u0, u1)

@@ -54,9 +54,13 @@ cudaError_t launch_finalize_batch(const SimArgs *inst, int n, cudaStream_t st);
 cudaError_t launch_wait_probe(const SimArgs &a, cudaStream_t st);
 
 // precision form of the solve (refine.cu)
+// gated: the kernel returns at once when the device-side stop test has passed
 cudaError_t launch_r64_residual(const SimArgs &a, const double *phi64, float *rr, float *dl,
-                                unsigned long long *maxr, cudaStream_t st);
-cudaError_t launch_r64_update(const SimArgs &a, double *phi64, const float *dl, cudaStream_t st);
+                                unsigned long long *maxr, cudaStream_t st, int gated = 0);
+cudaError_t launch_r64_update(const SimArgs &a, double *phi64, const float *dl, cudaStream_t st,
+                              int gated = 0);
+cudaError_t launch_r64_decide(const SimArgs &a, const unsigned long long *maxr, int sweeps, int mn,
+                              int mx, double tol, int write_stats, cudaStream_t st);
 cudaError_t launch_r64_field(const SimArgs &a, const double *phi64, cudaStream_t st);
 
 }  // namespace cupic

@@ -31,7 +31,8 @@ __device__ __forceinline__ double source64(const SimArgs &a, const long long *ac
 // r = b - A phi64 on interior rows (FP32 copy in rr, max |r| into *maxr as
 // the bits of a non-negative double); the correction dl is cleared
 __global__ void __launch_bounds__(kRBlock) k_r64_residual(SimArgs a, const double *phi64, float *rr,
-                                                         float *dl, unsigned long long *maxr) {
+                                                         float *dl, unsigned long long *maxr, int gated) {
+  if (gated && *reinterpret_cast<volatile int *>(&a.ctl->refine_done)) return;
   const int j = blockIdx.y, nnx = a.nnx, nny = a.nny;
   const size_t rb = (size_t)j * nnx;
   const long long *acc = reinterpret_cast<const long long *>(a.rho[a.ctl->cur]);
@@ -63,7 +64,8 @@ __global__ void __launch_bounds__(kRBlock) k_r64_residual(SimArgs a, const doubl
 }
 
 // phi64 += dl on interior rows; the FP32 potential follows
-__global__ void __launch_bounds__(kRBlock) k_r64_update(SimArgs a, double *phi64, const float *dl) {
+__global__ void __launch_bounds__(kRBlock) k_r64_update(SimArgs a, double *phi64, const float *dl, int gated) {
+  if (gated && *reinterpret_cast<volatile int *>(&a.ctl->refine_done)) return;
   const int j = blockIdx.y, nnx = a.nnx;
   const size_t rb = (size_t)j * nnx;
   for (int i = blockIdx.x * kRBlock + threadIdx.x; i < nnx; i += gridDim.x * kRBlock) {
@@ -73,6 +75,24 @@ __global__ void __launch_bounds__(kRBlock) k_r64_update(SimArgs a, double *phi64
       phi64[rb + i] = v;
     }
     a.phi[rb + i] = __double2float_rn(v);
+  }
+}
+
+// the stop test of the precision form after `sweeps` correction sweeps, on
+// the device: stop when the FP64 residual's max norm is below tol after at
+// least mn sweeps, or at mx sweeps; the first test that stops sets
+// refine_done (the later corrections then return at once) and records the
+// solve's sweeps and residual
+__global__ void k_r64_decide(Ctl *ctl, const unsigned long long *maxr, int sweeps, int mn, int mx,
+                             double tol, int write_stats) {
+  if (ctl->refine_done) return;
+  const double res = __longlong_as_double((long long)*maxr);
+  if ((sweeps >= mn && res < tol) || sweeps >= mx) {
+    ctl->refine_done = 1;
+    if (write_stats) {
+      ctl->sweeps = sweeps;
+      ctl->residual = (float)res;
+    }
   }
 }
 
@@ -103,15 +123,22 @@ dim3 row_grid(const SimArgs &a) { return dim3((a.nnx + kRBlock - 1) / kRBlock, a
 }  // namespace
 
 cudaError_t launch_r64_residual(const SimArgs &a, const double *phi64, float *rr, float *dl,
-                                unsigned long long *maxr, cudaStream_t st) {
+                                unsigned long long *maxr, cudaStream_t st, int gated) {
   cudaError_t e = cudaMemsetAsync(maxr, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
-  k_r64_residual<<<row_grid(a), kRBlock, 0, st>>>(a, phi64, rr, dl, maxr);
+  k_r64_residual<<<row_grid(a), kRBlock, 0, st>>>(a, phi64, rr, dl, maxr, gated);
   return cudaGetLastError();
 }
 
-cudaError_t launch_r64_update(const SimArgs &a, double *phi64, const float *dl, cudaStream_t st) {
-  k_r64_update<<<row_grid(a), kRBlock, 0, st>>>(a, phi64, dl);
+cudaError_t launch_r64_update(const SimArgs &a, double *phi64, const float *dl, cudaStream_t st,
+                              int gated) {
+  k_r64_update<<<row_grid(a), kRBlock, 0, st>>>(a, phi64, dl, gated);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_r64_decide(const SimArgs &a, const unsigned long long *maxr, int sweeps, int mn,
+                              int mx, double tol, int write_stats, cudaStream_t st) {
+  k_r64_decide<<<1, 1, 0, st>>>(a.ctl, maxr, sweeps, mn, mx, tol, write_stats);
   return cudaGetLastError();
 }
 
