@@ -974,8 +974,11 @@ int cupic_load_particles(cupic_ctx *c, int sp, const double *xyvv, int64_t n) {
   const size_t b_tmp = align256((size_t)n * sizeof(float4));
   const size_t b_h = align256((size_t)nb * ncy * sizeof(int32_t));
   const size_t b_in = mapped ? 0 : align256((size_t)n * 32);
+  // sized for a download of as many particles too, so that the download
+  // that usually follows does not grow it again
+  const size_t b_down = align256((ncy + 1) * sizeof(int64_t)) + (size_t)n * 32;
   void *scratch = nullptr;
-  CU(io_scratch(c, b_tmp + b_h + 256 + b_in, &scratch));
+  CU(io_scratch(c, std::max(b_tmp + b_h + 256 + b_in, b_down), &scratch));
   unsigned char *q = static_cast<unsigned char *>(scratch);
   float4 *tmp = reinterpret_cast<float4 *>(q);
   int32_t *H = reinterpret_cast<int32_t *>(q + b_tmp);
