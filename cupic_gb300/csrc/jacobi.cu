@@ -678,8 +678,6 @@ size_t jacobi_smem_bytes(int rows_per_cta, int depth, int pitch) {
   return (size_t)3 * (rows_per_cta + 2 * depth) * pitch * sizeof(float);
 }
 
-int jacobi_block() { return kJBlock; }
-
 // the attribute only grows, so contexts of different sizes can coexist
 cudaError_t jacobi_set_smem(size_t bytes) {
   static size_t cur = 0;

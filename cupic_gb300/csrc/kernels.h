@@ -31,7 +31,6 @@ cudaError_t launch_pack_rows(const SimArgs &a, int sp, const int64_t *off, float
                              double *out64, cudaStream_t st);
 
 size_t jacobi_smem_bytes(int rows_per_cta, int depth, int pitch);
-int jacobi_block();
 int jacobi_strip_rows(int nnx, int urows);
 cudaError_t jacobi_set_smem(size_t bytes);
 cudaError_t jacobi_max_ctas(size_t smem, int *per_sm);
