@@ -38,6 +38,8 @@ struct Ctl {
   uint32_t jepoch;        // solves run so far: the base of the halo words' epochs
   uint32_t idle;          // never written: the bounded-wait self-test waits on it
   int32_t refine_done;    // precision-form solve: the stop test passed, later corrections idle
+  uint32_t jdone;         // CTAs of the running solve that have finished (the last one resets it)
+  uint32_t pad;
   cupic_step_stats ring[kStatsRing];
 };
 

@@ -612,9 +612,15 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
     ctl->sweeps = done;
     ctl->residual = last;
   }
-  // the next solve's epochs; every CTA read the base before its first
-  // exchange, which CTA 0's last receive depended on
-  if (c == 0 && tid == 0) ctl->jepoch = ctl->jepoch + 1u;
+  // the next solve's epochs: the last CTA to finish advances the base, when
+  // every CTA of this solve has read it (each reads it first thing)
+  if (tid == 0) {
+    __threadfence();
+    if (atomicAdd(&ctl->jdone, 1u) == (unsigned)G - 1u) {
+      ctl->jdone = 0u;
+      atomicAdd(&ctl->jepoch, 1u);
+    }
+  }
 }
 
 __device__ __forceinline__ void jacobi_dispatch(const SimArgs &a, const JacobiArgs &J, int c, float *jsm,
