@@ -345,8 +345,11 @@ int tune_jacobi(cupic_ctx *c, int P, long long rows_fit) {
     c->jK = cd.G > 1 ? cd.K : 1;
     c->jP = P;
     c->jNoStrip = cd.nostrip;
+    // write_stats keeps the residual checks of the real solve (a solve with
+    // no tolerance that reports nothing skips them); the stats it writes
+    // are overwritten by the first real solve
     JacobiArgs J = jargs(c, 0.0, S, S, chk, 1);
-    J.write_stats = 0;
+    J.write_stats = 1;
     float t = 1e30f;
     bool ok = true;
     for (int rep = 0; rep < 3 && ok; ++rep) {
