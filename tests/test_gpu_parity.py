@@ -140,6 +140,20 @@ def test_jacobi_layouts(make_pair, monkeypatch, name, over, ctas, depth, strips)
     check_state(sim, ora)
 
 
+def test_repeated_short_solves_match_oracle(make_pair, monkeypatch):
+    """Back-to-back solves with one or two halo exchanges each: every solve
+    tags its halo words with new epochs, so no solve reads an earlier one's
+    rows."""
+    monkeypatch.setenv("CUPIC_JACOBI_DEPTH", "2")
+    sim, ora = make_pair("small", ctas=4)
+    sim.init_plasma()
+    ora.init_plasma()
+    for n in (3, 3, 5, 2, 3, 7, 4, 3):
+        sim.poisson_solver(1e-30, n, n, n)
+        ora.solve(1e-30, n, n, n)
+        np.testing.assert_array_equal(sim.phi().astype(np.float64), ora.phi(), err_msg=f"{n} sweeps")
+
+
 def test_stage_api_matches_oracle(make_pair):
     """Drive the reference's entry points one by one on a state loaded from
     host arrays (read_particle_file + the main loop, main.cu:59-96)."""
