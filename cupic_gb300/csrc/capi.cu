@@ -444,8 +444,9 @@ int refine_solve(cupic_ctx *c, double tol, int mn, int mx, int field, int write_
   unsigned long long *hbits = static_cast<unsigned long long *>(c->h_pin);
   int sweeps = 0;
   double res = 0.0;
+  CU(launch_r64_source(c->a, c->b64, c->stream));
   for (;;) {
-    CU(launch_r64_residual(c->a, c->phi64, c->rr, c->dl, c->maxr, c->stream));
+    CU(launch_r64_residual(c->a, c->phi64, c->b64, c->rr, c->maxr, c->stream));
     CU(cudaMemcpyAsync(hbits, c->maxr, sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                        c->stream));
     CU(cudaStreamSynchronize(c->stream));
@@ -454,13 +455,16 @@ int refine_solve(cupic_ctx *c, double tol, int mn, int mx, int field, int write_
     const int k = std::min(m, mx - sweeps);
     JacobiArgs J = jargs(c, 0.0, k, k, k, 0);
     J.write_stats = 0;
-    J.phi = c->dl;
+    J.phi = c->dl;  // the correction starts from zero
+    J.phi_zero = 1;
     J.src = c->rr;
     CU(launch_jacobi(c->a, J, c->stream));
     CU(launch_r64_update(c->a, c->phi64, c->dl, c->stream));
     sweeps += k;
   }
+  // the FP32 potential (and the field) from phi64
   if (field) CU(launch_r64_field(c->a, c->phi64, c->stream));
+  else CU(launch_r64_phi32(c->a, c->phi64, c->stream));
   if (write_stats) {
     struct {
       int32_t sweeps;
@@ -490,21 +494,25 @@ bool refine_on_device(const cupic_ctx *c, int mx) {
 int refine_solve_device(cupic_ctx *c, double tol, int mn, int mx, int field, int write_stats) {
   const int m = c->p.refine_every;
   CU(cudaMemsetAsync(&c->ctl->refine_done, 0, sizeof(int32_t), c->stream));
+  CU(launch_r64_source(c->a, c->b64, c->stream));
   for (int sweeps = 0;;) {
-    CU(launch_r64_residual(c->a, c->phi64, c->rr, c->dl, c->maxr, c->stream, 1));
+    CU(launch_r64_residual(c->a, c->phi64, c->b64, c->rr, c->maxr, c->stream, 1));
     CU(launch_r64_decide(c->a, c->maxr, sweeps, mn, mx, tol, write_stats, c->stream));
     if (sweeps >= mx) break;
     const int k = std::min(m, mx - sweeps);
     JacobiArgs J = jargs(c, 0.0, k, k, k, 0);
     J.write_stats = 0;
-    J.phi = c->dl;
+    J.phi = c->dl;  // the correction starts from zero
+    J.phi_zero = 1;
     J.src = c->rr;
     J.gated = 1;
     CU(launch_jacobi(c->a, J, c->stream));
     CU(launch_r64_update(c->a, c->phi64, c->dl, c->stream, 1));
     sweeps += k;
   }
+  // the FP32 potential (and the field) from phi64
   if (field) CU(launch_r64_field(c->a, c->phi64, c->stream));
+  else CU(launch_r64_phi32(c->a, c->phi64, c->stream));
   return CUPIC_OK;
 }
 
@@ -822,7 +830,7 @@ int cupic_create(const cupic_params *pin, int device, cupic_ctx **out) {
     return fail(CUPIC_ERR_NOMEM);
   a.ctl = c->ctl;
   if (c->p.refine_every > 0) {
-    if (dalloc(&c->phi64, nodes) || dalloc(&c->rr, nodes) || dalloc(&c->dl, nodes) ||
+    if (dalloc(&c->phi64, nodes) || dalloc(&c->b64, nodes) || dalloc(&c->rr, nodes) || dalloc(&c->dl, nodes) ||
         dalloc(&c->maxr, 1) || cudaMallocHost(&c->h_pin, 64) != cudaSuccess)
       return fail(CUPIC_ERR_NOMEM);
     if (cudaMemset(c->phi64, 0, nodes * sizeof(double))) return fail(CUPIC_ERR_CUDA);
@@ -863,6 +871,7 @@ int cupic_destroy(cupic_ctx *c) {
   cudaFree(c->jhalo);
   cudaFree(c->io_buf);
   cudaFree(c->phi64);
+  cudaFree(c->b64);
   cudaFree(c->rr);
   cudaFree(c->dl);
   cudaFree(c->maxr);

@@ -33,6 +33,7 @@ struct cupic_ctx {
   // precision form of the solve (refine_every > 0): FP64 potential, FP32
   // residual source and correction, the residual's max norm
   double *phi64 = nullptr;
+  double *b64 = nullptr;  // the FP64 source of the running solve
   float *rr = nullptr, *dl = nullptr;
   unsigned long long *maxr = nullptr;
   void *h_pin = nullptr;  // pinned: [0] max-norm bits, [1] {sweeps, residual}

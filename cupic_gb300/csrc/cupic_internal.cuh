@@ -95,6 +95,7 @@ struct JacobiArgs {
   int32_t write_stats;    // 1: store sweeps/residual in the control block
   int32_t zero_next;      // 1: also clear the next charge accumulator a.rho[cur^1] (a step's solve)
   int32_t gated;          // 1: return at once when ctl->refine_done is set (precision-form correction)
+  int32_t phi_zero;       // 1: the initial potential is zero everywhere and is not read
   unsigned int *flags;    // [G] last sweep published by each CTA
   unsigned int *bar;      // [1] grid barrier counter
   float *res_cta;         // [2*G] per-CTA max |dphi| of a checked sweep

@@ -350,7 +350,7 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
         if (k < total) {
           const int lr = k / nnx, i = k - lr * nnx, j = lo + lr;
           const size_t rb = (size_t)j * nnx;
-          v[u] = phi[rb + i];
+          v[u] = J.phi_zero ? 0.0f : phi[rb + i];
           if (j >= 1 && j <= nny - 2) {
             if (J.src) {
               bv[u] = J.src[rb + i];

@@ -54,8 +54,10 @@ cudaError_t launch_wait_probe(const SimArgs &a, cudaStream_t st);
 
 // precision form of the solve (refine.cu)
 // gated: the kernel returns at once when the device-side stop test has passed
-cudaError_t launch_r64_residual(const SimArgs &a, const double *phi64, float *rr, float *dl,
+cudaError_t launch_r64_source(const SimArgs &a, double *b64, cudaStream_t st);
+cudaError_t launch_r64_residual(const SimArgs &a, const double *phi64, const double *b64, float *rr,
                                 unsigned long long *maxr, cudaStream_t st, int gated = 0);
+cudaError_t launch_r64_phi32(const SimArgs &a, const double *phi64, cudaStream_t st);
 cudaError_t launch_r64_update(const SimArgs &a, double *phi64, const float *dl, cudaStream_t st,
                               int gated = 0);
 cudaError_t launch_r64_decide(const SimArgs &a, const unsigned long long *maxr, int sweeps, int mn,

@@ -28,17 +28,24 @@ __device__ __forceinline__ double source64(const SimArgs &a, const long long *ac
   return (double)f * a.cb;
 }
 
-// r = b - A phi64 on interior rows (FP32 copy in rr, max |r| into *maxr as
-// the bits of a non-negative double); the correction dl is cleared
-__global__ void __launch_bounds__(kRBlock) k_r64_residual(SimArgs a, const double *phi64, float *rr,
-                                                         float *dl, unsigned long long *maxr, int gated) {
-  if (gated && *reinterpret_cast<volatile int *>(&a.ctl->refine_done)) return;
+// the FP64 source of every node, once per solve (0 on the Dirichlet rows)
+__global__ void __launch_bounds__(kRBlock) k_r64_source(SimArgs a, double *b64) {
   const int j = blockIdx.y, nnx = a.nnx, nny = a.nny;
   const size_t rb = (size_t)j * nnx;
   const long long *acc = reinterpret_cast<const long long *>(a.rho[a.ctl->cur]);
+  for (int i = blockIdx.x * kRBlock + threadIdx.x; i < nnx; i += gridDim.x * kRBlock)
+    b64[rb + i] = (j == 0 || j == nny - 1) ? 0.0 : source64(a, acc, rb, i == nnx - 1 ? 0 : i);
+}
+
+// r = b - A phi64 on interior rows (FP32 copy in rr, max |r| into *maxr as
+// the bits of a non-negative double)
+__global__ void __launch_bounds__(kRBlock) k_r64_residual(SimArgs a, const double *phi64, const double *b64,
+                                                         float *rr, unsigned long long *maxr, int gated) {
+  if (gated && *reinterpret_cast<volatile int *>(&a.ctl->refine_done)) return;
+  const int j = blockIdx.y, nnx = a.nnx, nny = a.nny;
+  const size_t rb = (size_t)j * nnx;
   double m = 0.0;
   for (int i = blockIdx.x * kRBlock + threadIdx.x; i < nnx; i += gridDim.x * kRBlock) {
-    dl[rb + i] = 0.0f;
     if (j == 0 || j == nny - 1) {
       rr[rb + i] = 0.0f;
       continue;
@@ -48,7 +55,7 @@ __global__ void __launch_bounds__(kRBlock) k_r64_residual(SimArgs a, const doubl
     const double w = phi64[rb + (ii == 0 ? nnx - 2 : ii - 1)];
     const double e = phi64[rb + ii + 1];
     const double n = phi64[rb + nnx + ii], s = phi64[rb - nnx + ii];
-    const double r = source64(a, acc, rb, ii) - (4.0 * c - (((w + e) + n) + s));
+    const double r = b64[rb + ii] - (4.0 * c - (((w + e) + n) + s));
     rr[rb + i] = __double2float_rn(r);
     m = fmax(m, fabs(r));
   }
@@ -63,19 +70,22 @@ __global__ void __launch_bounds__(kRBlock) k_r64_residual(SimArgs a, const doubl
   }
 }
 
-// phi64 += dl on interior rows; the FP32 potential follows
+// phi64 += dl on interior rows (the FP32 potential follows once, at the end
+// of the solve)
 __global__ void __launch_bounds__(kRBlock) k_r64_update(SimArgs a, double *phi64, const float *dl, int gated) {
   if (gated && *reinterpret_cast<volatile int *>(&a.ctl->refine_done)) return;
   const int j = blockIdx.y, nnx = a.nnx;
+  if (j < 1 || j > a.nny - 2) return;
   const size_t rb = (size_t)j * nnx;
-  for (int i = blockIdx.x * kRBlock + threadIdx.x; i < nnx; i += gridDim.x * kRBlock) {
-    double v = phi64[rb + i];
-    if (j >= 1 && j <= a.nny - 2) {
-      v += (double)dl[rb + i];
-      phi64[rb + i] = v;
-    }
-    a.phi[rb + i] = __double2float_rn(v);
-  }
+  for (int i = blockIdx.x * kRBlock + threadIdx.x; i < nnx; i += gridDim.x * kRBlock)
+    phi64[rb + i] += (double)dl[rb + i];
+}
+
+// the FP32 potential from phi64, at the end of a solve
+__global__ void __launch_bounds__(kRBlock) k_r64_phi32(SimArgs a, const double *phi64) {
+  const size_t rb = (size_t)blockIdx.y * a.nnx;
+  for (int i = blockIdx.x * kRBlock + threadIdx.x; i < a.nnx; i += gridDim.x * kRBlock)
+    a.phi[rb + i] = __double2float_rn(phi64[rb + i]);
 }
 
 // the stop test of the precision form after `sweeps` correction sweeps, on
@@ -115,6 +125,7 @@ __global__ void __launch_bounds__(kRBlock) k_r64_field(SimArgs a, const double *
       ey = (phi64[k - nnx] - phi64[k + nnx]) / (2.0 * a.ds_d);
     }
     a.E[k] = make_float2(__double2float_rn(ex), __double2float_rn(ey));
+    a.phi[k] = __double2float_rn(phi64[k]);
   }
 }
 
@@ -122,11 +133,21 @@ dim3 row_grid(const SimArgs &a) { return dim3((a.nnx + kRBlock - 1) / kRBlock, a
 
 }  // namespace
 
-cudaError_t launch_r64_residual(const SimArgs &a, const double *phi64, float *rr, float *dl,
+cudaError_t launch_r64_source(const SimArgs &a, double *b64, cudaStream_t st) {
+  k_r64_source<<<row_grid(a), kRBlock, 0, st>>>(a, b64);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_r64_residual(const SimArgs &a, const double *phi64, const double *b64, float *rr,
                                 unsigned long long *maxr, cudaStream_t st, int gated) {
   cudaError_t e = cudaMemsetAsync(maxr, 0, sizeof(unsigned long long), st);
   if (e != cudaSuccess) return e;
-  k_r64_residual<<<row_grid(a), kRBlock, 0, st>>>(a, phi64, rr, dl, maxr, gated);
+  k_r64_residual<<<row_grid(a), kRBlock, 0, st>>>(a, phi64, b64, rr, maxr, gated);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_r64_phi32(const SimArgs &a, const double *phi64, cudaStream_t st) {
+  k_r64_phi32<<<row_grid(a), kRBlock, 0, st>>>(a, phi64);
   return cudaGetLastError();
 }
 
