@@ -18,7 +18,7 @@ __all__ = ["Sim", "Params", "StepStats", "workload_params", "load_library", "lib
            "CupicError", "params_from_input_data", "SPECIES", "FLAGS", "EXPORTED",
            "write_particles_file", "read_particles_file", "write_mesh_file",
            "write_bookmarks_file", "write_bins_file", "rewrite_input_data", "driver_path",
-           "Batch"]
+           "Batch", "reserve"]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
@@ -43,7 +43,7 @@ EXPORTED = [
     "cupic_mesh_snapshot", "cupic_save_bm", "cupic_save_bins", "cupic_load_particles_file",
     "cupic_batch_create", "cupic_batch_set", "cupic_batch_step", "cupic_batch_sync",
     "cupic_batch_destroy", "cupic_probe_current", "cupic_density_profile",
-    "cupic_test_bounded_wait",
+    "cupic_test_bounded_wait", "cupic_init_plasma_nowait", "cupic_reserve",
 ]
 
 
@@ -84,6 +84,8 @@ def load_library(build_if_missing=False):
         "cupic_create": [P(Params), c_i, P(vp)],
         "cupic_destroy": [vp],
         "cupic_init_plasma": [vp],
+        "cupic_init_plasma_nowait": [vp],
+        "cupic_reserve": [c_i, ctypes.c_uint64, c_i32],
         "cupic_load_particles": [vp, c_i, P(c_d), c_i64],
         "cupic_set_time": [vp, c_i64, c_d, c_d, c_d],
         "cupic_get_time": [vp, P(c_i64), P(c_d), P(c_d), P(c_d)],
@@ -207,6 +209,13 @@ def rewrite_input_data(path, n_ini):
     _ok(load_library().cupic_rewrite_input_data(os.fsencode(path), n_ini), "rewrite_input_data")
 
 
+def reserve(nbytes, contexts=0, device=0):
+    """Grows the device memory pool the contexts allocate from to at least
+    nbytes and the kept streams to `contexts` contexts' worth (see
+    cupic_reserve)."""
+    _ok(load_library().cupic_reserve(device, int(nbytes), int(contexts)), "reserve")
+
+
 def params_from_input_data(path):
     """Parse the reference's input_data file (init.cu:424-789)."""
     p = Params()
@@ -247,8 +256,13 @@ class Sim:
         return self.p.nnx * self.p.nny
 
     # ---- setup ------------------------------------------------------------
-    def init_plasma(self):
-        _ok(self.L.cupic_init_plasma(self.h), "init_plasma")
+    def init_plasma(self, wait=True):
+        """init_sim (init.cu:57-83); wait=False only enqueues it on the
+        context's stream (call sync() before reading results)."""
+        if wait:
+            _ok(self.L.cupic_init_plasma(self.h), "init_plasma")
+        else:
+            _ok(self.L.cupic_init_plasma_nowait(self.h), "init_plasma_nowait")
 
     def load(self, species, xyvv):
         a = np.ascontiguousarray(xyvv, dtype=np.float64).reshape(-1, 4)

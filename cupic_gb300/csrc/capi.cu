@@ -38,11 +38,29 @@ int cuda_status(cudaError_t e) {
   return CUPIC_ERR_CUDA;
 }
 
+// A context's device memory comes from the device's stream-ordered pool,
+// allocated and freed in the order of the context's stream: creating or
+// destroying a context never waits for the device (other contexts may be
+// stepping), and a server reuses the memory of finished requests.
 template <class T>
-cudaError_t dalloc(T **p, size_t n) {
+cudaError_t dalloc(cupic_ctx *c, T **p, size_t n) {
   *p = nullptr;
   if (n == 0) n = 1;
-  return cudaMalloc((void **)p, n * sizeof(T));
+  return cudaMallocAsync((void **)p, n * sizeof(T), c->stream);
+}
+
+void dfree(cupic_ctx *c, void *p) {
+  if (p) cudaFreeAsync(p, c->stream);
+}
+
+// the default pool keeps freed memory for the next allocation instead of
+// returning it to the system at every synchronisation
+cudaError_t keep_pool(int device) {
+  cudaMemPool_t pool;
+  cudaError_t e = cudaDeviceGetDefaultMemPool(&pool, device);
+  if (e != cudaSuccess) return e;
+  uint64_t keep = UINT64_MAX;
+  return cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
 }
 
 // The device address of a host buffer that kernels can read in place
@@ -61,11 +79,10 @@ void *mapped_host(const void *p) {
 // uploads and downloads allocate nothing)
 cudaError_t io_scratch(cupic_ctx *c, size_t bytes, void **out) {
   if (bytes > c->io_cap) {
-    cudaStreamSynchronize(c->stream);
-    cudaFree(c->io_buf);
+    dfree(c, c->io_buf);
     c->io_buf = nullptr;
     c->io_cap = 0;
-    cudaError_t e = cudaMalloc(&c->io_buf, bytes);
+    cudaError_t e = dalloc(c, reinterpret_cast<unsigned char **>(&c->io_buf), bytes);
     if (e != cudaSuccess) return e;
     c->io_cap = bytes;
   }
@@ -75,21 +92,58 @@ cudaError_t io_scratch(cupic_ctx *c, size_t bytes, void **out) {
 
 size_t align256(size_t v) { return (v + 255) / 256 * 256; }
 
+// The streams and events of destroyed contexts, kept per device for the
+// next contexts: creating a stream can stall for tens of milliseconds while
+// the device is busy, which a server admitting requests cannot afford.
+struct StreamSet {
+  cudaStream_t stream, side;
+  cudaEvent_t fork, join;
+};
+std::mutex g_streams_mu;
+std::vector<std::vector<StreamSet>> g_streams;
+
+cudaError_t new_stream_set(StreamSet *s) {
+  *s = {};
+  cudaError_t e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->join, cudaEventDisableTiming);
+  return e;
+}
+
+void keep_stream_set(int device, const StreamSet &s) {
+  std::lock_guard<std::mutex> lk(g_streams_mu);
+  if ((int)g_streams.size() <= device) g_streams.resize(device + 1);
+  g_streams[device].push_back(s);
+}
+
+cudaError_t take_stream_set(int device, StreamSet *s) {
+  {
+    std::lock_guard<std::mutex> lk(g_streams_mu);
+    if ((int)g_streams.size() > device && !g_streams[device].empty()) {
+      *s = g_streams[device].back();
+      g_streams[device].pop_back();
+      return cudaSuccess;
+    }
+  }
+  return new_stream_set(s);
+}
+
 int32_t round8(double v) { return (int32_t)((((int64_t)ceil(v)) + 7) / 8 * 8); }
 
-void free_species(SpeciesDev &S) {
-  cudaFree(S.parts);
-  cudaFree(S.seg);
-  cudaFree(S.cap);
-  cudaFree(S.cnt);
-  cudaFree(S.nstay);
-  cudaFree(S.nup);
-  cudaFree(S.ndown);
-  cudaFree(S.stage_up);
-  cudaFree(S.stage_down);
-  cudaFree(S.inj_tin);
-  cudaFree(S.inj_p);
-  cudaFree(S.inj_d);
+void free_species(cupic_ctx *c, SpeciesDev &S) {
+  dfree(c, S.parts);
+  dfree(c, S.seg);
+  dfree(c, S.cap);
+  dfree(c, S.cnt);
+  dfree(c, S.nstay);
+  dfree(c, S.nup);
+  dfree(c, S.ndown);
+  dfree(c, S.stage_up);
+  dfree(c, S.stage_down);
+  dfree(c, S.inj_tin);
+  dfree(c, S.inj_p);
+  dfree(c, S.inj_d);
   memset(&S, 0, sizeof(S));
 }
 
@@ -104,7 +158,7 @@ int layout_species(cupic_ctx *c, int sp, const std::vector<int32_t> &capv) {
   SpeciesDev &S = c->a.sp[sp];
   const int ncy = c->p.ncy;
   const int inj_cap = S.inj_cap;
-  free_species(S);
+  free_species(c, S);
   S.inj_cap = inj_cap;
   c->cap[sp] = capv;
   c->seg[sp].assign(ncy, 0);
@@ -117,24 +171,32 @@ int layout_species(cupic_ctx *c, int sp, const std::vector<int32_t> &capv) {
   }
   c->total_cap[sp] = tot;
   S.stage_cap = round8(cmax * c->p.stage_frac) + 64;
-  CU(dalloc(&S.parts, (size_t)tot));
-  CU(dalloc(&S.seg, ncy));
-  CU(dalloc(&S.cap, ncy));
-  CU(dalloc(&S.cnt, ncy));
-  CU(dalloc(&S.nstay, ncy));
-  CU(dalloc(&S.nup, ncy));
-  CU(dalloc(&S.ndown, ncy));
-  CU(dalloc(&S.stage_up, (size_t)ncy * S.stage_cap));
-  CU(dalloc(&S.stage_down, (size_t)ncy * S.stage_cap));
-  CU(dalloc(&S.inj_tin, (size_t)S.inj_cap));
-  CU(dalloc(&S.inj_p, (size_t)S.inj_cap));
-  CU(dalloc(&S.inj_d, (size_t)S.inj_cap));
-  CU(cudaMemcpy(S.seg, c->seg[sp].data(), ncy * sizeof(int64_t), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(S.cap, capv.data(), ncy * sizeof(int32_t), cudaMemcpyHostToDevice));
-  CU(cudaMemset(S.cnt, 0, ncy * sizeof(int32_t)));
-  CU(cudaMemset(S.nstay, 0, ncy * sizeof(int32_t)));
-  CU(cudaMemset(S.nup, 0, ncy * sizeof(int32_t)));
-  CU(cudaMemset(S.ndown, 0, ncy * sizeof(int32_t)));
+  CU(dalloc(c, &S.parts, (size_t)tot));
+  CU(dalloc(c, &S.seg, ncy));
+  CU(dalloc(c, &S.cap, ncy));
+  CU(dalloc(c, &S.cnt, ncy));
+  CU(dalloc(c, &S.nstay, ncy));
+  CU(dalloc(c, &S.nup, ncy));
+  CU(dalloc(c, &S.ndown, ncy));
+  CU(dalloc(c, &S.stage_up, (size_t)ncy * S.stage_cap));
+  CU(dalloc(c, &S.stage_down, (size_t)ncy * S.stage_cap));
+  CU(dalloc(c, &S.inj_tin, (size_t)S.inj_cap));
+  CU(dalloc(c, &S.inj_p, (size_t)S.inj_cap));
+  CU(dalloc(c, &S.inj_d, (size_t)S.inj_cap));
+  const bool uniform = std::all_of(capv.begin(), capv.end(), [&](int32_t v) { return v == capv[0]; });
+  if (uniform) {
+    // filled on the context's stream: no host wait
+    CU(launch_uniform_layout(S, ncy, capv.empty() ? 0 : capv[0], c->stream));
+  } else {
+    CU(cudaStreamSynchronize(c->stream));
+    CU(cudaMemcpy(S.seg, c->seg[sp].data(), ncy * sizeof(int64_t), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(S.cap, capv.data(), ncy * sizeof(int32_t), cudaMemcpyHostToDevice));
+    CU(cudaMemset(S.cnt, 0, ncy * sizeof(int32_t)));
+    CU(cudaMemset(S.nstay, 0, ncy * sizeof(int32_t)));
+    CU(cudaMemset(S.nup, 0, ncy * sizeof(int32_t)));
+    CU(cudaMemset(S.ndown, 0, ncy * sizeof(int32_t)));
+    CU(cudaDeviceSynchronize());
+  }
   destroy_graph(c);
   return CUPIC_OK;
 }
@@ -215,15 +277,15 @@ int jacobi_rows(const cupic_ctx *c, int G, int K, int P, long long rows_fit) {
 }
 
 int alloc_jacobi_scratch(cupic_ctx *c, int G, long long GK, int P) {
-  cudaFree(c->jflags);
-  cudaFree(c->jres);
-  cudaFree(c->jhalo);
+  dfree(c, c->jflags);
+  dfree(c, c->jres);
+  dfree(c, c->jhalo);
   c->jflags = nullptr;
   c->jres = nullptr;
   c->jhalo = nullptr;
-  CU(dalloc(&c->jflags, (size_t)G + 1));
-  CU(dalloc(&c->jres, (size_t)2 * G));
-  CU(dalloc(&c->jhalo, (size_t)4 * GK * P));
+  CU(dalloc(c, &c->jflags, (size_t)G + 1));
+  CU(dalloc(c, &c->jres, (size_t)2 * G));
+  CU(dalloc(c, &c->jhalo, (size_t)4 * GK * P));
   // epoch 0 is never valid; the solves on the context's stream follow the clearing
   CU(cudaMemsetAsync(c->jhalo, 0, sizeof(unsigned long long) * 4 * (size_t)GK * P, c->stream));
   return CUPIC_OK;
@@ -419,6 +481,7 @@ JacobiArgs jargs(const cupic_ctx *c, double tol, int mn, int mx, int chk, int fi
 
 int set_phi_both(cupic_ctx *c, const double *phi) {
   const size_t n = (size_t)c->a.nnx * c->a.nny;
+  CU(cudaStreamSynchronize(c->stream));  // no kernel of the context still uses phi
   std::vector<float> h(n);
   for (size_t k = 0; k < n; ++k) h[k] = (float)phi[k];
   CU(cudaMemcpy(c->a.phi, h.data(), n * sizeof(float), cudaMemcpyHostToDevice));
@@ -426,13 +489,9 @@ int set_phi_both(cupic_ctx *c, const double *phi) {
   return CUPIC_OK;
 }
 
-int set_linear_phi(cupic_ctx *c) {
-  const int nnx = c->a.nnx, nny = c->a.nny;
-  std::vector<double> h((size_t)nnx * nny);
-  for (int j = 0; j < nny; ++j)
-    for (int i = 0; i < nnx; ++i)  // init.cu:235-241
-      h[(size_t)j * nnx + i] = (1.0 - (double)j / (double)c->p.ncy) * c->p.phi_p;
-  return set_phi_both(c, h.data());
+int set_linear_phi(cupic_ctx *c) {  // init.cu:235-241, on the device
+  CU(launch_linear_phi(c->a, c->p.phi_p, c->phi64, c->stream));
+  return CUPIC_OK;
 }
 
 // Precision form (refine_every = m > 0): every m FP32 Jacobi sweeps on the
@@ -815,29 +874,38 @@ int cupic_create(const cupic_params *pin, int device, cupic_ctx **out) {
     return r;
   };
   if (cudaSetDevice(device) != cudaSuccess) return fail(CUPIC_ERR_CUDA);
-  if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+  if (cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      keep_pool(device) != cudaSuccess)
     return fail(CUPIC_ERR_CUDA);
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming) != cudaSuccess)
-    return fail(CUPIC_ERR_CUDA);
+  {
+    StreamSet s{};
+    const cudaError_t e = take_stream_set(device, &s);
+    c->stream = s.stream;
+    c->side = s.side;
+    c->ev_fork = s.fork;
+    c->ev_join = s.join;
+    if (e != cudaSuccess) return fail(CUPIC_ERR_CUDA);
+  }
   fill_constants(c);
   SimArgs &a = c->a;
   const size_t nodes = (size_t)a.nnx * a.nny;
-  if (dalloc(&a.phi, nodes) || dalloc(&a.E, nodes) || dalloc(&a.rho[0], nodes) ||
-      dalloc(&a.rho[1], nodes) || dalloc(&c->ctl, 1))
+  if (dalloc(c, &a.phi, nodes) || dalloc(c, &a.E, nodes) || dalloc(c, &a.rho[0], nodes) ||
+      dalloc(c, &a.rho[1], nodes) || dalloc(c, &c->ctl, 1))
     return fail(CUPIC_ERR_NOMEM);
   a.ctl = c->ctl;
   if (c->p.refine_every > 0) {
-    if (dalloc(&c->phi64, nodes) || dalloc(&c->b64, nodes) || dalloc(&c->rr, nodes) || dalloc(&c->dl, nodes) ||
-        dalloc(&c->maxr, 1) || cudaMallocHost(&c->h_pin, 64) != cudaSuccess)
+    if (dalloc(c, &c->phi64, nodes) || dalloc(c, &c->b64, nodes) || dalloc(c, &c->rr, nodes) || dalloc(c, &c->dl, nodes) ||
+        dalloc(c, &c->maxr, 1) || cudaMallocHost(&c->h_pin, 64) != cudaSuccess)
       return fail(CUPIC_ERR_NOMEM);
-    if (cudaMemset(c->phi64, 0, nodes * sizeof(double))) return fail(CUPIC_ERR_CUDA);
+    if (cudaMemsetAsync(c->phi64, 0, nodes * sizeof(double), c->stream)) return fail(CUPIC_ERR_CUDA);
   }
-  if (cudaMemset(a.phi, 0, nodes * sizeof(float)) || cudaMemset(a.E, 0, nodes * sizeof(float2)) ||
-      cudaMemset(a.rho[0], 0, nodes * 8) || cudaMemset(a.rho[1], 0, nodes * 8) ||
-      cudaMemset(c->ctl, 0, sizeof(Ctl)))
+  // set-up is ordered on the context's stream: creating a context never
+  // waits for the device, which may be busy with other contexts' steps
+  if (cudaMemsetAsync(a.phi, 0, nodes * sizeof(float), c->stream) ||
+      cudaMemsetAsync(a.E, 0, nodes * sizeof(float2), c->stream) ||
+      cudaMemsetAsync(a.rho[0], 0, nodes * 8, c->stream) ||
+      cudaMemsetAsync(a.rho[1], 0, nodes * 8, c->stream) ||
+      cudaMemsetAsync(c->ctl, 0, sizeof(Ctl), c->stream))
     return fail(CUPIC_ERR_CUDA);
   const int32_t capj = round8(c->p.ppr * (1.0 + c->p.row_slack)) + 64;
   for (int sp = 0; sp < 2; ++sp) {
@@ -859,28 +927,36 @@ int cupic_destroy(cupic_ctx *c) {
   if (!c) return CUPIC_ERR_ARG;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
-  destroy_graph(c);
-  for (int sp = 0; sp < 2; ++sp) free_species(c->a.sp[sp]);
-  cudaFree(c->a.phi);
-  cudaFree(c->a.E);
-  cudaFree(c->a.rho[0]);
-  cudaFree(c->a.rho[1]);
-  cudaFree(c->ctl);
-  cudaFree(c->jflags);
-  cudaFree(c->jres);
-  cudaFree(c->jhalo);
-  cudaFree(c->io_buf);
-  cudaFree(c->phi64);
-  cudaFree(c->b64);
-  cudaFree(c->rr);
-  cudaFree(c->dl);
-  cudaFree(c->maxr);
-  if (c->h_pin) cudaFreeHost(c->h_pin);
   if (c->side) cudaStreamSynchronize(c->side);
-  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
-  if (c->ev_join) cudaEventDestroy(c->ev_join);
-  if (c->side) cudaStreamDestroy(c->side);
-  if (c->stream) cudaStreamDestroy(c->stream);
+  destroy_graph(c);
+  // stream-ordered frees on the context's stream, which the streams'
+  // destruction below lets finish
+  for (int sp = 0; sp < 2; ++sp) free_species(c, c->a.sp[sp]);
+  dfree(c, c->a.phi);
+  dfree(c, c->a.E);
+  dfree(c, c->a.rho[0]);
+  dfree(c, c->a.rho[1]);
+  dfree(c, c->ctl);
+  dfree(c, c->jflags);
+  dfree(c, c->jres);
+  dfree(c, c->jhalo);
+  dfree(c, c->io_buf);
+  dfree(c, c->phi64);
+  dfree(c, c->b64);
+  dfree(c, c->rr);
+  dfree(c, c->dl);
+  dfree(c, c->maxr);
+  if (c->h_pin) cudaFreeHost(c->h_pin);
+  if (c->stream && c->side && c->ev_fork && c->ev_join) {
+    // back to the device's set for the next context (the frees above run
+    // on the stream, before any later work the next owner enqueues)
+    keep_stream_set(c->device, {c->stream, c->side, c->ev_fork, c->ev_join});
+  } else {
+    if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->side) cudaStreamDestroy(c->side);
+    if (c->stream) cudaStreamDestroy(c->stream);
+  }
   delete c;
   return CUPIC_OK;
 }
@@ -888,15 +964,8 @@ int cupic_destroy(cupic_ctx *c) {
 int cupic_set_time(cupic_ctx *c, int64_t step, double t, double tin_e, double tin_i) {
   if (!c) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
-  CU(cudaStreamSynchronize(c->stream));
-  struct {
-    int64_t step;
-    double t;
-    double tin[2];
-    int32_t tin_set[2];
-  } h = {step, t, {tin_e, tin_i}, {tin_e >= 0 ? 1 : 0, tin_i >= 0 ? 1 : 0}};
-  static_assert(sizeof(h) == offsetof(Ctl, cur), "Ctl layout");
-  CU(cudaMemcpy(c->ctl, &h, sizeof(h), cudaMemcpyHostToDevice));
+  // ordered on the context's stream after the work already enqueued there
+  CU(launch_set_time(c->ctl, step, t, tin_e, tin_i, c->stream));
   return CUPIC_OK;
 }
 
@@ -918,8 +987,9 @@ int cupic_get_time(cupic_ctx *c, int64_t *step, double *t, double *tin_e, double
   return CUPIC_OK;
 }
 
-int cupic_init_plasma(cupic_ctx *c) {
-  if (!c) return CUPIC_ERR_ARG;
+// init_sim's n_ini == 0 branch (init.cu:70-83), enqueued on the context's
+// stream without waiting for it
+int init_plasma_enqueue(cupic_ctx *c) {
   CU(cudaSetDevice(c->device));
   const int capj = c->cap[0].empty() ? 0 : *std::min_element(c->cap[0].begin(), c->cap[0].end());
   if (capj < c->p.ppr) return CUPIC_ERR_CAPACITY;
@@ -932,12 +1002,50 @@ int cupic_init_plasma(cupic_ctx *c) {
   rc = run_solve(c, p.init_tol, p.init_min_sweeps, p.init_max_sweeps, p.check_every, 1);
   if (rc) return rc;
   CU(launch_leapfrog_start(c->a, c->stream));
-  rc = sync_check(c);
-  if (rc) return rc;
   rc = cupic_set_time(c, (int64_t)p.n_ini + 1, p.n_ini * p.dt + p.dt, -1.0, -1.0);
   if (rc) return rc;
   c->initialized = true;
-  return finish(c);
+  return CUPIC_OK;
+}
+
+int cupic_init_plasma(cupic_ctx *c) {
+  if (!c) return CUPIC_ERR_ARG;
+  const int rc = init_plasma_enqueue(c);
+  return rc ? rc : finish(c);
+}
+
+int cupic_reserve(int device, uint64_t bytes, int32_t contexts) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev || contexts < 0) {
+    cudaGetLastError();
+    return CUPIC_ERR_ARG;
+  }
+  CU(cudaSetDevice(device));
+  CU(keep_pool(device));
+  int have = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_streams_mu);
+    if ((int)g_streams.size() > device) have = (int)g_streams[device].size();
+  }
+  for (int k = have; k < contexts; ++k) {
+    StreamSet s{};
+    CU(new_stream_set(&s));
+    keep_stream_set(device, s);
+  }
+  if (bytes == 0) return CUPIC_OK;
+  cudaStream_t st = nullptr;
+  CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+  void *p = nullptr;
+  cudaError_t e = cudaMallocAsync(&p, (size_t)bytes, st);
+  if (e == cudaSuccess) e = cudaFreeAsync(p, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cudaStreamDestroy(st);
+  return e == cudaSuccess ? CUPIC_OK : cuda_status(e);
+}
+
+int cupic_init_plasma_nowait(cupic_ctx *c) {
+  if (!c) return CUPIC_ERR_ARG;
+  return init_plasma_enqueue(c);
 }
 
 int cupic_init_mesh(cupic_ctx *c) {

@@ -20,6 +20,10 @@ cudaError_t launch_inject_append(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_finalize(const SimArgs &a, cudaStream_t st);
 size_t push_smem_bytes(int nnx, int pb = 256);  // pb: threads per block (256 single context)
 cudaError_t push_set_smem(size_t bytes);
+// set-up on the context's stream
+cudaError_t launch_uniform_layout(const SpeciesDev &S, int ncy, int capj, cudaStream_t st);
+cudaError_t launch_set_time(Ctl *ctl, int64_t step, double t, double tin_e, double tin_i, cudaStream_t st);
+cudaError_t launch_linear_phi(const SimArgs &a, double phi_p, double *phi64, cudaStream_t st);
 
 int load_blocks(int64_t n, int num_sms);
 cudaError_t launch_load_hist(const SimArgs &a, const double *in, int64_t n, int nb, float4 *tmp,

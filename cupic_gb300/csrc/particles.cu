@@ -227,6 +227,40 @@ __global__ void k_deposit(SimArgs a) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// set-up kernels, so that a context's set-up is ordered on its own stream
+// and never waits on the host for the device
+// ---------------------------------------------------------------------------
+// uniform row layout: segment j at j*capj, capacity capj, no particles
+__global__ void k_uniform_layout(SpeciesDev S, int ncy, int capj) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < ncy; j += gridDim.x * blockDim.x) {
+    S.seg[j] = (int64_t)j * capj;
+    S.cap[j] = capj;
+    S.cnt[j] = S.nstay[j] = S.nup[j] = S.ndown[j] = 0;
+  }
+}
+
+// the clocks of the control block (the first fields of Ctl)
+__global__ void k_set_time(Ctl *ctl, int64_t step, double t, double tin_e, double tin_i) {
+  ctl->step = step;
+  ctl->t = t;
+  ctl->tin[0] = tin_e;
+  ctl->tin[1] = tin_i;
+  ctl->tin_set[0] = tin_e >= 0 ? 1 : 0;
+  ctl->tin_set[1] = tin_i >= 0 ? 1 : 0;
+}
+
+// phi = (1 - j/ncy) phi_p on node row j (init.cu:235-241), in FP64, the
+// FP32 copy rounded from it
+__global__ void k_linear_phi(SimArgs a, double phi_p, double *phi64) {
+  const int j = blockIdx.y;
+  const double v = __dmul_rn(__dsub_rn(1.0, __ddiv_rn((double)j, (double)a.ncy)), phi_p);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.nnx; i += gridDim.x * blockDim.x) {
+    a.phi[(size_t)j * a.nnx + i] = (float)v;
+    if (phi64) phi64[(size_t)j * a.nnx + i] = v;
+  }
+}
+
 // zero the accumulator the next deposit writes (rho[cur^1])
 __global__ void k_zero_next_rho(SimArgs a) {
   unsigned long long *r = a.rho[a.ctl->cur ^ 1];
@@ -754,6 +788,21 @@ cudaError_t launch_zero_next_rho(const SimArgs &a, cudaStream_t st) {
   int blocks = (int)((n + 1023) / 1024);
   if (blocks > 1184) blocks = 1184;
   k_zero_next_rho<<<blocks, 1024, 0, st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_uniform_layout(const SpeciesDev &S, int ncy, int capj, cudaStream_t st) {
+  k_uniform_layout<<<(ncy + 255) / 256, 256, 0, st>>>(S, ncy, capj);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_time(Ctl *ctl, int64_t step, double t, double tin_e, double tin_i, cudaStream_t st) {
+  k_set_time<<<1, 1, 0, st>>>(ctl, step, t, tin_e, tin_i);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_linear_phi(const SimArgs &a, double phi_p, double *phi64, cudaStream_t st) {
+  k_linear_phi<<<dim3((a.nnx + 255) / 256, a.nny), 256, 0, st>>>(a, phi_p, phi64);
   return cudaGetLastError();
 }
 

@@ -9,8 +9,9 @@ steps: the net charge absorbed by the probe per step, ions minus electrons.
 Continuous batching (``serve_batched``): requests that have arrived are
 admitted while their footprint (16 B per particle plus 12 B per cell) fits
 the HBM budget and a slot is free; their state is created and initialised
-on the device while the running members step, and they join the batch at
-the next tick.  A tick is one ``Batch.step`` of all members (at most `tick`
+on the device while the running members step (creation and initialisation
+are enqueued on the request's own stream and never wait for the device),
+and they join the batch at the next tick.  A tick is one ``Batch.step`` of all members (at most `tick`
 steps, never past a member's last step); members that finish leave the
 batch and free their footprint.  A member's result is bit-identical to the
 one it gets alone, because batched and solo steps compute the same thing.
@@ -21,7 +22,7 @@ import time
 
 import numpy as np
 
-from . import Batch, Sim
+from . import Batch, Sim, reserve
 from .params import footprint_bytes
 
 
@@ -68,6 +69,13 @@ def serve_batched(requests, budget_bytes=96 << 30, max_slots=512, tick=50, devic
     """Runs the requests with continuous batching in real time; fills in
     start, finish and current of every request and returns them."""
     warm_plans(requests, device)
+    # the memory pool holds what the admitted requests can use at once (a
+    # context takes about three times its admission footprint: row slack,
+    # staging rows, mesh arrays) and the kept streams serve as many
+    # contexts, so that admissions during the run neither map new pages nor
+    # create streams
+    need = sum(sorted((footprint_bytes(r.params) for r in requests), reverse=True)[:max_slots])
+    reserve(min(budget_bytes, 3 * need), min(max_slots, len(requests)), device)
     pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
     queue = collections.deque()
     active = []   # [request, sim, steps done]
@@ -93,7 +101,7 @@ def serve_batched(requests, budget_bytes=96 << 30, max_slots=512, tick=50, devic
                     break
                 r = queue.popleft()
                 sim = Sim(r.params, device=device)
-                sim.init_plasma()
+                sim.init_plasma(wait=False)  # on its own stream, beside the batch
                 r.start = clock() - t0
                 joining.append([r, sim, 0])
                 used += fp
@@ -106,6 +114,8 @@ def serve_batched(requests, budget_bytes=96 << 30, max_slots=512, tick=50, devic
                 r.current = probe_current(sim, r.window)
                 r.finish = clock() - t0
             if done or joining:
+                for a in joining:
+                    a[1].sync()  # its initialisation is complete before the batch uses it
                 active = [a for a in active if a[2] < a[0].steps] + joining
                 joining = []
                 batch.set([a[1] for a in active])

@@ -144,6 +144,23 @@ const char *cupic_strerror(int status);
  * plasma, linear phi, deposit, initial solve, field, leapfrog half-step. */
 int cupic_init_plasma(struct cupic_ctx *ctx);
 
+/* The same, enqueued on the context's stream without waiting for it (a
+ * server admits a request while the device steps others).  Device-side
+ * conditions are reported by the next call that waits (cupic_sync,
+ * cupic_step's status, ...).  cupic_create itself never waits for the
+ * device when the solver layout of its mesh shape is already known. */
+int cupic_init_plasma_nowait(struct cupic_ctx *ctx);
+
+/* Contexts take their device memory from the device's stream-ordered pool
+ * (cudaMallocAsync), which keeps freed memory for later contexts, and their
+ * streams from a per-device set that destroyed contexts return theirs to.
+ * This grows the pool to at least `bytes` and the set to `contexts` streams'
+ * worth now, so that contexts created later (a server admitting requests
+ * while the device steps others) neither map new pages nor create streams,
+ * which can stall while the device is busy.  Both are kept until the
+ * process exits. */
+int cupic_reserve(int device, uint64_t bytes, int32_t contexts);
+
 /* Replaces one species with n particles given as the reference's particle
  * struct (4 doubles x,y,vx,vy; stdh.h:30-36), in any order; they are binned
  * by y row keeping the given order within a row (init.cu:400-407).

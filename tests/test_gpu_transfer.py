@@ -69,3 +69,26 @@ def test_repeated_transfers_reuse_scratch(gpu_lib):
             np.testing.assert_array_equal(np.sort(back, axis=0), np.sort(part.astype(np.float32).astype(np.float64), axis=0))
     finally:
         sim.close()
+
+
+def test_nowait_init_matches_waiting_init(gpu_lib):
+    """init_plasma enqueued without waiting (a server's admission) leaves
+    the same state as the waiting call once the context is synchronised."""
+    p = cg.workload_params("tiny")
+    a, b = cg.Sim(p), cg.Sim(p)
+    try:
+        a.init_plasma()
+        b.init_plasma(wait=False)
+        b.sync()
+        assert a.get_time() == b.get_time()
+        for sp in (0, 1):
+            np.testing.assert_array_equal(a.particles(sp), b.particles(sp))
+        np.testing.assert_array_equal(a.phi(), b.phi())
+        a.step(3)
+        b.step(3)
+        for sp in (0, 1):
+            np.testing.assert_array_equal(a.particles(sp), b.particles(sp))
+        assert a.stats(1)[0]["live"] == b.stats(1)[0]["live"]
+    finally:
+        a.close()
+        b.close()
