@@ -36,8 +36,21 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s full PIC cycle"
 UNIT = "particle-steps/s"
 STATS_BYTES = 96
-# kernels launched per step: jacobi, zero, push, arrive, inject sched/gen/append, finalize
-KERNELS_PER_STEP = 8
+# kernels launched per step: jacobi (which also clears the next charge),
+# push, arrive, inject sched/gen/append, finalize
+KERNELS_PER_STEP = 7
+
+
+def kernels_per_step(p):
+    """Kernels one step launches.  The precision form replaces the solve by
+    the FP64 source, per correction up to the sweep cap a residual, a stop
+    test, a Jacobi launch and an update (the ones after the stop test return
+    at once), a last residual and test, and the field; its step also clears
+    the next charge with its own kernel."""
+    if p.refine_every <= 0:
+        return KERNELS_PER_STEP
+    corrections = -(-max(p.max_sweeps, 0) // p.refine_every)
+    return (KERNELS_PER_STEP - 1) + 1 + 1 + 4 * corrections + 2 + 1
 
 # algorithmic bytes per unit of work (FP32 SoA, 16 B state per particle)
 PUSH_BYTES_PER_PARTICLE = 32      # 16 B read + 16 B write
@@ -399,7 +412,7 @@ def run_cupic(args, world, rank, local):
                        "jacobi_plan": dict(zip(("ctas", "rows_per_cta", "halo_depth"),
                                                sim.solver_plan()))},
             "e2e": e2e,
-            "gpu_launches": KERNELS_PER_STEP * args.steps,
+            "gpu_launches": kernels_per_step(p) * args.steps,
             "roofline": dominant,
             "roofline_other": other,
             "phases_ms_per_step": {k: v / args.steps for k, v in phases.items()},
