@@ -92,3 +92,24 @@ def test_nowait_init_matches_waiting_init(gpu_lib):
     finally:
         a.close()
         b.close()
+
+
+def test_reused_streams_and_pool_give_identical_runs(gpu_lib):
+    """Contexts created after others were destroyed reuse their streams and
+    pooled memory; every run still gives the same bits."""
+    cg.reserve(1 << 28, contexts=4)
+    p = cg.workload_params("tiny")
+    ref = None
+    for k in range(6):
+        sim = cg.Sim(p)
+        try:
+            sim.init_plasma(wait=(k % 2 == 0))
+            sim.step(4)
+            got = [sim.particles(sp) for sp in (0, 1)] + [sim.phi()]
+        finally:
+            sim.close()
+        if ref is None:
+            ref = got
+        else:
+            for a, b in zip(ref, got):
+                np.testing.assert_array_equal(a, b)
