@@ -205,9 +205,29 @@ class ClockSampler:
 # CPU oracle (the reference algorithm restated) on a strip of the workload
 # ---------------------------------------------------------------------------
 
-def cpu_strip(p, rows_req, steps, warmup, target_s=1.0):
+def cpu_model():
+    """The host CPU's model name (lscpu, else /proc/cpuinfo), or None."""
+    import subprocess
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return None
+
+
+def cpu_strip(p, rows_req, steps, warmup, target_s=1.0, threads=None):
     from oracle import oracle as O
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
     O.set_threads(threads)
     rows = rows_req
     if rows <= 0:
@@ -246,6 +266,8 @@ def run_reference(args, world, rank):
         return 0
     p = make_params(args)
     cb = cpu_strip(p, args.cpu_rows, args.steps, args.warmup)
+    # one thread on a small strip for a few steps, beside the all-core figure
+    one = cpu_strip(p, 64, 2, 1, threads=1)
     line = {
         "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup,
@@ -257,6 +279,8 @@ def run_reference(args, world, rank):
         "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
         "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
+        "cpu": {"model": cpu_model(), "nproc": os.cpu_count(),
+                "single_thread": {"value": one["value"], "unit": UNIT, "sample": one["sample"]}},
     }
     print(json.dumps(line), flush=True)
     return 0
