@@ -533,9 +533,38 @@ __device__ __forceinline__ void arrive_row(const SimArgs &a, const int d, const 
 
 __global__ void k_arrive(SimArgs a) { arrive_row(a, blockIdx.x, blockIdx.y); }
 
-__global__ void k_arrive_batch(const SimArgs *__restrict__ inst, const int2 *__restrict__ work) {
-  const int2 w = work[blockIdx.x];
-  arrive_row(inst[w.x], w.y, blockIdx.y);
+// many contexts: one warp per (row, species) task t = 2 * work index +
+// species, eight per block -- most rows of a batch move few particles, so a
+// block per row would be mostly set-up
+constexpr int kArriveWarps = 8;
+__global__ void __launch_bounds__(32 * kArriveWarps)
+    k_arrive_batch(const SimArgs *__restrict__ inst, const int2 *__restrict__ work, int ntask) {
+  const int t = blockIdx.x * kArriveWarps + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (t >= ntask) return;
+  const int2 w = work[t >> 1];
+  const SimArgs &a = inst[w.x];
+  const int d = w.y, sp = t & 1;
+  const SpeciesDev &S = a.sp[sp];
+  const int ns = S.nstay[d];
+  const int nb = d > 0 ? S.nup[d - 1] : 0;
+  const int na = d + 1 < a.ncy ? S.ndown[d + 1] : 0;
+  const int capd = S.cap[d];
+  float4 *row = S.parts + S.seg[d];
+  if (nb) {
+    const float4 *up = S.stage_up + (size_t)(d - 1) * S.stage_cap;
+    for (int k = lane; k < nb; k += 32)
+      if (ns + k < capd) row[ns + k] = up[k];
+  }
+  if (na) {
+    const float4 *dn = S.stage_down + (size_t)(d + 1) * S.stage_cap;
+    for (int k = lane; k < na; k += 32)
+      if (ns + nb + k < capd) row[ns + nb + k] = dn[k];
+  }
+  if (lane == 0) {
+    const int tot = ns + nb + na;
+    if (tot > capd) raise_flags(a.ctl, CUPIC_FLAG_CAPACITY);
+    S.cnt[d] = min(tot, capd);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -876,7 +905,10 @@ cudaError_t launch_push_deposit_batch(const SimArgs *inst, const int2 *row_work,
 }
 
 cudaError_t launch_arrive_batch(const SimArgs *inst, const int2 *row_work, int n, cudaStream_t st) {
-  k_arrive_batch<<<dim3(n, 2), 128, 0, st>>>(inst, row_work);
+  if (n == 0) return cudaSuccess;
+  const int ntask = 2 * n;
+  k_arrive_batch<<<(ntask + kArriveWarps - 1) / kArriveWarps, 32 * kArriveWarps, 0, st>>>(inst, row_work,
+                                                                                        ntask);
   return cudaGetLastError();
 }
 
