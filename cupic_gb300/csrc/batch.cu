@@ -47,7 +47,7 @@ struct cupic_batch {
          cap_halo = 0;
   int ngroups = 0, nctas = 0, nrows = 0, max_nnx = 0, max_ncy = 0, max_inj = 0;
   // d_rows: rows of short-row instances (ncx <= kShortRow, pushed by
-  // 256-thread blocks), then rows of mid-size ones (512-thread blocks),
+  // 128-thread blocks), then rows of mid-size ones (512-thread blocks),
   // then rows of big ones (ncy >= kBigRows), which are pushed by the
   // single-context kernel, one launch per instance on parallel branches
   int nrows_short = 0, nrows_mid = 0, max_nnx_short = 0, max_nnx_mid = 0;
@@ -61,7 +61,7 @@ struct cupic_batch {
 
 namespace {
 
-constexpr int kShortRow = 64;  // cells per row up to which 256-thread blocks push a row
+constexpr int kShortRow = 64;  // cells per row up to which 128-thread blocks push a row
 constexpr int kBigRows = 512;  // rows from which an instance fills the GPU by itself
 constexpr int kPushBranches = 4;
 
@@ -315,7 +315,7 @@ int enqueue(cupic_batch *b) {
       CU(launch_push_deposit(b->members[b->big[q]]->a, b->push_st[q % nbr]));
     for (int k = 0; k < nbr; ++k) CU(cudaEventRecord(b->ev_push_join[k], b->push_st[k]));
   }
-  CU(launch_push_deposit_batch(b->d_inst, b->d_rows, b->nrows_short, b->max_nnx_short, 256, st));
+  CU(launch_push_deposit_batch(b->d_inst, b->d_rows, b->nrows_short, b->max_nnx_short, 128, st));
   CU(launch_push_deposit_batch(b->d_inst, b->d_rows + b->nrows_short, b->nrows_mid, b->max_nnx_mid,
                                512, st));
   for (int k = 0; k < nbr; ++k) CU(cudaStreamWaitEvent(st, b->ev_push_join[k], 0));

@@ -486,10 +486,11 @@ __global__ void __launch_bounds__(kPB, 4) k_push_deposit(SimArgs a) {
 }
 
 // many contexts in one launch: block 2b + sp pushes species sp of work[b] =
-// {instance, row}; PB = 256 for short rows (more blocks per SM), 512
+// {instance, row}; PB = 128 for short rows (eight blocks per SM: a short
+// row's unit is mostly set-up, which more resident blocks overlap), 512
 // otherwise
 template <int PB>
-__global__ void __launch_bounds__(PB, PB == 256 ? 4 : 2)
+__global__ void __launch_bounds__(PB, PB == 128 ? 8 : (PB == 256 ? 4 : 2))
     k_push_deposit_batch(const SimArgs *__restrict__ inst, const int2 *__restrict__ work) {
   extern __shared__ __align__(128) unsigned char push_raw[];
   // the instance's arguments in shared memory: read there as needed instead
@@ -900,6 +901,7 @@ cudaError_t push_batch(const SimArgs *inst, const int2 *row_work, int n, int max
 cudaError_t launch_push_deposit_batch(const SimArgs *inst, const int2 *row_work, int n, int max_nnx,
                                       int threads, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
+  if (threads == 128) return push_batch<128>(inst, row_work, n, max_nnx, st);
   return threads == 256 ? push_batch<256>(inst, row_work, n, max_nnx, st)
                         : push_batch<512>(inst, row_work, n, max_nnx, st);
 }
