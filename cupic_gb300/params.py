@@ -2,7 +2,7 @@
 
 The fields are the reference's normalised input_data parameters
 (src/init.cu:451-789 of AntonioTejero/cupic) plus the Jacobi stop rule and
-storage knobs of this build.  ``workload_params`` builds the parameter sets
+the storage knobs of the GPU layout.  ``workload_params`` builds the parameter sets
 of the named workloads directly in normalised units.
 """
 import ctypes

@@ -47,7 +47,7 @@ def check(p, ref):
     assert math.sqrt(2.0 * PI * p.me / p.kte) / (p.n * lx * p.ds) == h(ref["dtin_e"])
     assert math.sqrt(2.0 * PI * p.mi / p.kti) / (p.n * lx * p.ds) == h(ref["dtin_i"])
     # particles per species, int(n*Lx*ds*ds)*ncy in 32-bit int (init.cu:136).
-    # The reference's product wraps past 2^31 (defect D16); this build keeps
+    # The reference's product wraps past 2^31 (defect D16); the library keeps
     # the exact product, whose low 32 bits must match.
     exact = p.ppr * p.ncy
     wrapped = (exact + 2 ** 31) % 2 ** 32 - 2 ** 31
