@@ -2,8 +2,8 @@
  * pic_oracle.cpp -- CPU oracle of the cupic per-step PIC cycle.
  *
  * TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py use it as the checker.  The product path
- * never links it.
+ * CPU-baseline leg of bench.py use it to check and time against.  The
+ * product path never links it.
  *
  * Parity: pinned.  The input_data normalisation is checked bit for bit
  * against the reference's own init_* getters compiled from its sources

@@ -3,9 +3,9 @@
  *
  * TEST INFRASTRUCTURE ONLY.  The oracle is a CPU restatement of the
  * reference cycle (AntonioTejero/cupic, src/mesh.cu, src/particles.cu,
- * src/cc.cu, src/init.cu) used by tests/, __graft_entry__.smoke() and the
- * CPU-baseline leg of bench.py as the checker.  Nothing in the product path
- * (cupic_gb300/) links or calls it.
+ * src/cc.cu, src/init.cu) that tests/, __graft_entry__.smoke() and the
+ * CPU-baseline leg of bench.py check and time against.  Nothing in the
+ * product path (cupic_gb300/) links or calls it.
  *
  * Two precisions share one code path:
  *   fp64=1  all-FP64 "precision oracle": double particles, double charge
