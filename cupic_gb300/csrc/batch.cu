@@ -91,7 +91,10 @@ void drop_graph(cupic_batch *b) {
 }
 
 // the batched solve's layout of one instance: the fewest CTAs whose shared
-// memory holds its rows, with a halo depth of up to 8
+// memory holds its rows, with a halo depth of up to kBatchDepth (over the
+// 256-instance mix, depths of 2, 3, 4, 6, 8 and 16 gave 15.1, 14.6, 14.4,
+// 14.8, 14.6 and 16.1 ms per batched step)
+constexpr int kBatchDepth = 4;
 struct Plan {
   int G, B, K, P;
   size_t smem;
@@ -106,7 +109,7 @@ bool plan_instance(const SimArgs &a, long long rows_fit, Plan *out) {
   }
   for (int G = 2; G <= M; ++G) {
     const int B = (M + G - 1) / G;
-    const int K = std::min(8, M / G);
+    const int K = std::min(kBatchDepth, M / G);
     if (K >= 1 && B + 2 * K <= rows_fit) {
       *out = {G, B, K, P, jacobi_smem_bytes(B, K, P)};
       return true;
