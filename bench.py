@@ -37,8 +37,8 @@ METRIC = "particle-steps/s full PIC cycle"
 UNIT = "particle-steps/s"
 STATS_BYTES = 96
 # kernels launched per step: jacobi (which also clears the next charge),
-# push, arrive, inject sched/gen/append, finalize
-KERNELS_PER_STEP = 7
+# push, room check, arrive, inject sched/gen/append, finalize
+KERNELS_PER_STEP = 8
 
 
 def kernels_per_step(p):

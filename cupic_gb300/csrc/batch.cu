@@ -11,12 +11,16 @@
 //   - push, arrive and the charge clear: work lists of {instance, row};
 //     instances of 512 rows or more, which fill the GPU by themselves, are
 //     pushed by the single-context kernel on parallel graph branches;
-//   - the injection draws (beside the push, on a side stream), the append
-//     and the bookkeeping: one block or thread per instance and species.
+//   - the injection draws (beside the push, on a side stream), the room
+//     check, the append and the bookkeeping: one block or thread per
+//     instance and species.
 // Every kernel reads its instance's SimArgs from a device array, so members
 // keep their own buffers and control blocks, and a member's results are the
 // ones it gets when stepped alone.  The step is captured once per
-// membership as a CUDA graph.
+// membership as a CUDA graph.  A member whose rows run out of room halts
+// alone (its kernels return at once); the batch's sync grows its rows and
+// completes its steps with the single-context step, and the next batched
+// step rebuilds the arrays.
 #include <string.h>
 
 #include <algorithm>
@@ -34,6 +38,7 @@ struct cupic_batch {
   cudaStream_t stream = nullptr, side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::vector<cupic_ctx *> members;
+  std::vector<int> epochs;  // members' layout epochs when the arrays were built
   // device arrays, grown as needed
   SimArgs *d_inst = nullptr;
   JacobiArgs *d_jargs = nullptr;
@@ -121,6 +126,8 @@ bool plan_instance(const SimArgs &a, long long rows_fit, Plan *out) {
 int build(cupic_batch *b) {
   drop_graph(b);
   const int n = (int)b->members.size();
+  b->epochs.clear();
+  for (const cupic_ctx *c : b->members) b->epochs.push_back(c->layout_epoch);
   if (n == 0) return CUPIC_OK;
   int dev_max = 0;
   CU(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device));
@@ -322,8 +329,9 @@ int enqueue(cupic_batch *b) {
   CU(launch_push_deposit_batch(b->d_inst, b->d_rows + b->nrows_short, b->nrows_mid, b->max_nnx_mid,
                                512, st));
   for (int k = 0; k < nbr; ++k) CU(cudaStreamWaitEvent(st, b->ev_push_join[k], 0));
-  CU(launch_arrive_batch(b->d_inst, b->d_rows, b->nrows, st));
   CU(cudaStreamWaitEvent(st, b->ev_join, 0));
+  CU(launch_room_batch(b->d_inst, n, b->max_ncy, st));
+  CU(launch_arrive_batch(b->d_inst, b->d_rows, b->nrows, st));
   CU(launch_inject_append_batch(b->d_inst, n, b->max_ncy, st));
   CU(launch_finalize_batch(b->d_inst, n, st));
   return CUPIC_OK;
@@ -402,6 +410,15 @@ int cupic_batch_step(cupic_batch *b, int32_t nsteps) {
   if (!b || nsteps < 0) return CUPIC_ERR_ARG;
   if (b->members.empty() || nsteps == 0) return CUPIC_OK;
   CU(cudaSetDevice(b->device));
+  // a member whose rows grew (its run halted and was completed alone) has
+  // new buffers
+  for (size_t i = 0; i < b->members.size(); ++i)
+    if (b->members[i]->layout_epoch != b->epochs[i]) {
+      CU(cudaStreamSynchronize(b->stream));
+      const int rc = build(b);
+      if (rc) return rc;
+      break;
+    }
   if (!b->graph_ok) {
     int rc = capture(b);
     if (rc) return rc;

@@ -29,6 +29,13 @@ namespace {
     if (e_ != cudaSuccess) return cuda_status(e_); \
   } while (0)
 
+// waits for the context's work, completing a run that ran out of room
+#define SETTLE(c)              \
+  do {                         \
+    const int rc_ = settle(c); \
+    if (rc_) return rc_;       \
+  } while (0)
+
 int cuda_status(cudaError_t e) {
   if (e == cudaErrorMemoryAllocation) {
     cudaGetLastError();
@@ -629,8 +636,12 @@ int flag_status(uint32_t f) {
   return CUPIC_OK;
 }
 
+int settle(cupic_ctx *c);
+
 int finish(cupic_ctx *c) {
-  int rc = sync_check(c);
+  int rc = settle(c);
+  if (rc) return rc;
+  rc = sync_check(c);
   if (rc) return rc;
   uint32_t f = 0;
   rc = read_ctl_flags(c, &f);
@@ -648,8 +659,9 @@ int enqueue_after_solve(cupic_ctx *c, bool zeroed) {
   CU(cudaEventRecord(c->ev_join, c->side));
   if (!zeroed) CU(launch_zero_next_rho(c->a, c->stream));
   CU(launch_push_deposit(c->a, c->stream));
-  CU(launch_arrive(c->a, c->stream));
   CU(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
+  CU(launch_room(c->a, c->stream));
+  CU(launch_arrive(c->a, c->stream));
   CU(launch_inject_append(c->a, c->stream));
   CU(launch_finalize(c->a, c->stream));
   return CUPIC_OK;
@@ -686,9 +698,173 @@ int capture_step(cupic_ctx *c) {
   return CUPIC_OK;
 }
 
+// n steps, graph-launched where the step is captured
+int launch_steps(cupic_ctx *c, int64_t n) {
+  if (n <= 0) return CUPIC_OK;
+  if (!c->graph_ok) {
+    int rc = capture_step(c);
+    if (rc) return rc;
+  }
+  for (int64_t i = 0; i < n; ++i) {
+    if (c->graph_ok) {
+      CU(cudaGraphLaunch(c->graph, c->stream));
+    } else {
+      int rc = enqueue_step(c);
+      if (rc) return rc;
+    }
+    c->host_cur ^= 1;
+  }
+  return CUPIC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// rows that run out of room (the room check of particles.cu halts the run)
+// ---------------------------------------------------------------------------
+int read_i32(const int32_t *src, int64_t n, std::vector<int32_t> &out) {
+  out.assign((size_t)std::max<int64_t>(n, 0), 0);
+  if (n > 0) CU(cudaMemcpy(out.data(), src, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost));
+  return CUPIC_OK;
+}
+
+// Gives every row j of species sp that cannot hold need[j] particles the
+// capacity need[j] * (1 + row_slack) + 64, in a new particle array, and
+// moves the first keep[j] particles of every row (keep: a device array)
+// there in order.  Other rows keep their capacity.  The stream is idle.
+int fit_rows(cupic_ctx *c, int sp, const std::vector<int64_t> &need, const int32_t *keep) {
+  SpeciesDev &S = c->a.sp[sp];
+  const int ncy = c->p.ncy;
+  std::vector<int32_t> capv = c->cap[sp];
+  bool grow = false;
+  for (int j = 0; j < ncy; ++j)
+    if (need[j] > capv[j]) {
+      const double want = (double)need[j] * (1.0 + c->p.row_slack) + 64.0;
+      if (want > 2.0e9) return CUPIC_ERR_CAPACITY;
+      capv[j] = round8(want);
+      grow = true;
+    }
+  if (!grow) return CUPIC_OK;
+  std::vector<int64_t> seg(ncy);
+  int64_t tot = 0;
+  for (int j = 0; j < ncy; ++j) {
+    seg[j] = tot;
+    tot += capv[j];
+  }
+  float4 *parts = nullptr;
+  int64_t *dseg = nullptr;
+  int32_t *dcap = nullptr;
+  cudaError_t e = dalloc(c, &parts, (size_t)tot);
+  if (e == cudaSuccess) e = dalloc(c, &dseg, (size_t)ncy);
+  if (e == cudaSuccess) e = dalloc(c, &dcap, (size_t)ncy);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dseg, seg.data(), ncy * sizeof(int64_t), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(dcap, capv.data(), ncy * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = launch_move_rows(S.parts, S.seg, parts, dseg, keep, ncy, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {  // the old layout stays
+    dfree(c, parts);
+    dfree(c, dseg);
+    dfree(c, dcap);
+    cudaStreamSynchronize(c->stream);
+    return cuda_status(e);
+  }
+  dfree(c, S.parts);
+  dfree(c, S.seg);
+  dfree(c, S.cap);
+  S.parts = parts;
+  S.seg = dseg;
+  S.cap = dcap;
+  c->cap[sp] = capv;
+  c->seg[sp] = seg;
+  c->total_cap[sp] = tot;
+  destroy_graph(c);  // the captured launches hold the old pointers
+  ++c->layout_epoch;
+  return CUPIC_OK;
+}
+
+// staging rows sized for the largest row, once the staged movers of the
+// running step have arrived (the frees are ordered after the arrivals)
+int fit_staging(cupic_ctx *c, int sp) {
+  SpeciesDev &S = c->a.sp[sp];
+  const int ncy = c->p.ncy;
+  const int32_t cmax = c->cap[sp].empty() ? 0 : *std::max_element(c->cap[sp].begin(), c->cap[sp].end());
+  const int32_t want = round8(cmax * c->p.stage_frac) + 64;
+  if (want <= S.stage_cap) return CUPIC_OK;
+  float4 *up = nullptr, *down = nullptr;
+  cudaError_t e = dalloc(c, &up, (size_t)ncy * want);
+  if (e == cudaSuccess) e = dalloc(c, &down, (size_t)ncy * want);
+  if (e != cudaSuccess) {  // the old staging rows stay
+    dfree(c, up);
+    return cuda_status(e);
+  }
+  dfree(c, S.stage_up);
+  dfree(c, S.stage_down);
+  S.stage_up = up;
+  S.stage_down = down;
+  S.stage_cap = want;
+  destroy_graph(c);
+  ++c->layout_epoch;
+  return CUPIC_OK;
+}
+
+// A run halted by the room check: the halted step has pushed and deposited,
+// its movers sit in the staging rows and its injected particles in inj_p.
+// Grow the rows that cannot take them, complete the step, then run the
+// steps that returned at once (skipped counts the halted step too).
+int complete_halted(cupic_ctx *c, int32_t skipped) {
+  const int ncy = c->p.ncy;
+  int32_t ne[2] = {0, 0};
+  CU(cudaMemcpy(ne, c->ctl->inj_gen, sizeof(ne), cudaMemcpyDeviceToHost));
+  for (int sp = 0; sp < 2; ++sp) {
+    const SpeciesDev &S = c->a.sp[sp];
+    std::vector<int32_t> ns, nu, nd, dst;
+    int rc = read_i32(S.nstay, ncy, ns);
+    if (!rc) rc = read_i32(S.nup, ncy, nu);
+    if (!rc) rc = read_i32(S.ndown, ncy, nd);
+    if (!rc) rc = read_i32(S.inj_d, std::min(ne[sp], S.inj_cap), dst);
+    if (rc) return rc;
+    std::vector<int64_t> need(ncy);
+    for (int j = 0; j < ncy; ++j)
+      need[j] = (int64_t)ns[j] + (j > 0 ? nu[j - 1] : 0) + (j + 1 < ncy ? nd[j + 1] : 0);
+    for (int32_t d : dst)
+      if (d >= 0 && d < ncy) ++need[d];
+    rc = fit_rows(c, sp, need, S.nstay);
+    if (rc) return rc;
+  }
+  CU(cudaMemsetAsync(&c->ctl->halt, 0, sizeof(int32_t), c->stream));
+  CU(cudaMemsetAsync(&c->ctl->skipped, 0, sizeof(int32_t), c->stream));
+  CU(launch_arrive(c->a, c->stream));
+  CU(launch_inject_append(c->a, c->stream));
+  CU(launch_finalize(c->a, c->stream));
+  for (int sp = 0; sp < 2; ++sp) {
+    const int rc = fit_staging(c, sp);
+    if (rc) return rc;
+  }
+  int32_t cur = 0;
+  CU(cudaStreamSynchronize(c->stream));
+  CU(cudaMemcpy(&cur, &c->ctl->cur, sizeof(cur), cudaMemcpyDeviceToHost));
+  c->host_cur = cur;
+  return launch_steps(c, (int64_t)skipped - 1);
+}
+
+// Waits for the context's work; a run that the room check halted is
+// completed first, as often as it halts again.
+int settle(cupic_ctx *c) {
+  for (;;) {
+    CU(cudaStreamSynchronize(c->stream));
+    int32_t hs[2];
+    static_assert(offsetof(Ctl, skipped) == offsetof(Ctl, halt) + 4, "Ctl layout");
+    CU(cudaMemcpy(hs, &c->ctl->halt, sizeof(hs), cudaMemcpyDeviceToHost));
+    if (!hs[0]) return CUPIC_OK;
+    const int rc = complete_halted(c, hs[1]);
+    if (rc) return rc;
+  }
+}
+
 int get_row_counts(cupic_ctx *c, int sp, std::vector<int32_t> &cnt) {
   cnt.resize(c->p.ncy);
-  CU(cudaStreamSynchronize(c->stream));
+  int rc = settle(c);
+  if (rc) return rc;
   CU(cudaMemcpy(cnt.data(), c->a.sp[sp].cnt, c->p.ncy * sizeof(int32_t), cudaMemcpyDeviceToHost));
   return CUPIC_OK;
 }
@@ -972,7 +1148,7 @@ int cupic_set_time(cupic_ctx *c, int64_t step, double t, double tin_e, double ti
 int cupic_get_time(cupic_ctx *c, int64_t *step, double *t, double *tin_e, double *tin_i) {
   if (!c) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
-  CU(cudaStreamSynchronize(c->stream));
+  SETTLE(c);
   struct {
     int64_t step;
     double t;
@@ -993,6 +1169,9 @@ int init_plasma_enqueue(cupic_ctx *c) {
   CU(cudaSetDevice(c->device));
   const int capj = c->cap[0].empty() ? 0 : *std::min_element(c->cap[0].begin(), c->cap[0].end());
   if (capj < c->p.ppr) return CUPIC_ERR_CAPACITY;
+  // a halted run that was never completed is discarded with the old state
+  static_assert(offsetof(Ctl, skipped) == offsetof(Ctl, halt) + 4, "Ctl layout");
+  CU(cudaMemsetAsync(&c->ctl->halt, 0, 2 * sizeof(int32_t), c->stream));
   CU(launch_init_particles(c->a, c->stream));
   int rc = set_linear_phi(c);
   if (rc) return rc;
@@ -1084,7 +1263,7 @@ int cupic_get_solver_plan(cupic_ctx *c, int32_t *ctas, int32_t *rows_per_cta, in
 int cupic_load_particles(cupic_ctx *c, int sp, const double *xyvv, int64_t n) {
   if (!c || sp < 0 || sp > 1 || n < 0 || (n > 0 && !xyvv)) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
-  CU(cudaStreamSynchronize(c->stream));
+  SETTLE(c);
   const int ncy = c->p.ncy;
   const int nb = load_blocks(n, c->num_sms);
   // a mapped host array is read in place by the conversion kernel (as fast
@@ -1191,7 +1370,28 @@ int cupic_particle_mover(cupic_ctx *c) {
   CU(cudaSetDevice(c->device));
   CU(launch_zero_next_rho(c->a, c->stream));
   CU(launch_push_deposit(c->a, c->stream));
+  // rows that cannot take their stayers and the movers staged for them
+  // grow first (the step's graph does this with the room check)
+  CU(cudaStreamSynchronize(c->stream));
+  const int ncy = c->p.ncy;
+  for (int sp = 0; sp < 2; ++sp) {
+    const SpeciesDev &S = c->a.sp[sp];
+    std::vector<int32_t> ns, nu, nd;
+    int rc = read_i32(S.nstay, ncy, ns);
+    if (!rc) rc = read_i32(S.nup, ncy, nu);
+    if (!rc) rc = read_i32(S.ndown, ncy, nd);
+    if (rc) return rc;
+    std::vector<int64_t> need(ncy);
+    for (int j = 0; j < ncy; ++j)
+      need[j] = (int64_t)ns[j] + (j > 0 ? nu[j - 1] : 0) + (j + 1 < ncy ? nd[j + 1] : 0);
+    rc = fit_rows(c, sp, need, S.nstay);
+    if (rc) return rc;
+  }
   CU(launch_arrive(c->a, c->stream));
+  for (int sp = 0; sp < 2; ++sp) {
+    const int rc = fit_staging(c, sp);
+    if (rc) return rc;
+  }
   c->rho_valid = false;  // until cc completes the next charge
   return finish(c);
 }
@@ -1200,9 +1400,27 @@ int cupic_cc(cupic_ctx *c, double t) {
   if (!c) return CUPIC_ERR_ARG;
   if (!c->initialized) return CUPIC_ERR_STATE;
   CU(cudaSetDevice(c->device));
-  CU(cudaStreamSynchronize(c->stream));
+  SETTLE(c);
   CU(cudaMemcpy(&c->ctl->t, &t, sizeof(double), cudaMemcpyHostToDevice));
-  CU(launch_inject(c->a, c->stream));
+  CU(launch_inject_draw(c->a, c->stream));
+  // rows that cannot take the injected particles grow first
+  CU(cudaStreamSynchronize(c->stream));
+  const int ncy = c->p.ncy;
+  int32_t ne[2] = {0, 0};
+  CU(cudaMemcpy(ne, c->ctl->inj_gen, sizeof(ne), cudaMemcpyDeviceToHost));
+  for (int sp = 0; sp < 2; ++sp) {
+    const SpeciesDev &S = c->a.sp[sp];
+    std::vector<int32_t> cnt, dst;
+    int rc = read_i32(S.cnt, ncy, cnt);
+    if (!rc) rc = read_i32(S.inj_d, std::min(ne[sp], S.inj_cap), dst);
+    if (rc) return rc;
+    std::vector<int64_t> need(cnt.begin(), cnt.end());
+    for (int32_t d : dst)
+      if (d >= 0 && d < ncy) ++need[d];
+    rc = fit_rows(c, sp, need, S.cnt);
+    if (rc) return rc;
+  }
+  CU(launch_inject_append(c->a, c->stream));
   CU(launch_finalize(c->a, c->stream));
   c->host_cur ^= 1;
   c->rho_valid = true;
@@ -1218,28 +1436,17 @@ int cupic_step(cupic_ctx *c, int32_t nsteps) {
     if (rc) return rc;
   }
   if (c->p.refine_every > 0 && !refine_on_device(c, c->p.max_sweeps)) {
-    // the solve reads its residual norm on the host: no graph
+    // the solve reads its residual norm on the host: no graph, and a step
+    // that runs out of room is completed before the next one starts
     for (int i = 0; i < nsteps; ++i) {
       int rc = enqueue_step(c);
+      if (!rc) c->host_cur ^= 1;
+      if (!rc) rc = settle(c);
       if (rc) return rc;
-      c->host_cur ^= 1;
     }
     return CUPIC_OK;
   }
-  if (!c->graph_ok) {
-    int rc = capture_step(c);
-    if (rc) return rc;
-  }
-  for (int i = 0; i < nsteps; ++i) {
-    if (c->graph_ok) {
-      CU(cudaGraphLaunch(c->graph, c->stream));
-    } else {
-      int rc = enqueue_step(c);
-      if (rc) return rc;
-    }
-    c->host_cur ^= 1;
-  }
-  return CUPIC_OK;
+  return launch_steps(c, nsteps);
 }
 
 int cupic_sync(cupic_ctx *c) {
@@ -1304,8 +1511,8 @@ int cupic_step_timed(cupic_ctx *c, int32_t nsteps, float *phase_ms, int32_t npha
   cudaError_t e = rc ? cudaErrorUnknown : cudaEventRecord(ev[0], c->stream);
   for (int s = 0; s < nsteps && e == cudaSuccess; ++s) {
     // the launch order of enqueue_step, with an event after each
-    // main-stream kernel; the inject phase is the wait for the side branch
-    // (draws) plus the append
+    // main-stream kernel; the arrive phase is the wait for the side branch
+    // (draws), the room check and the arrivals
     cudaEvent_t *q = &ev[(size_t)s * per + 1];
     if (c->p.refine_every > 0) {
       const int r = run_solve(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1);
@@ -1323,9 +1530,10 @@ int cupic_step_timed(cupic_ctx *c, int32_t nsteps, float *phase_ms, int32_t npha
     if (e == cudaSuccess) e = cudaEventRecord(q[1], c->stream);
     if (e == cudaSuccess) e = launch_push_deposit(c->a, c->stream);
     if (e == cudaSuccess) e = cudaEventRecord(q[2], c->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_join, 0);
+    if (e == cudaSuccess) e = launch_room(c->a, c->stream);
     if (e == cudaSuccess) e = launch_arrive(c->a, c->stream);
     if (e == cudaSuccess) e = cudaEventRecord(q[3], c->stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_join, 0);
     if (e == cudaSuccess) e = launch_inject_append(c->a, c->stream);
     if (e == cudaSuccess) e = cudaEventRecord(q[4], c->stream);
     if (e == cudaSuccess) e = launch_finalize(c->a, c->stream);
@@ -1375,7 +1583,7 @@ int cupic_get_rho_fixed(cupic_ctx *c, int which, int64_t *acc) {
     int rc = deposit_current(c);
     if (rc) return rc;
   }
-  CU(cudaStreamSynchronize(c->stream));
+  SETTLE(c);
   const size_t nodes = (size_t)c->a.nnx * c->a.nny;
   CU(cudaMemcpy(acc, c->a.rho[c->host_cur ^ which], nodes * sizeof(int64_t), cudaMemcpyDeviceToHost));
   return CUPIC_OK;
@@ -1402,7 +1610,7 @@ int cupic_get_rho(cupic_ctx *c, int which, double *rho) {
 int cupic_get_phi_f32(cupic_ctx *c, float *phi) {
   if (!c || !phi) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
-  CU(cudaStreamSynchronize(c->stream));
+  SETTLE(c);
   CU(cudaMemcpy(phi, c->a.phi, sizeof(float) * (size_t)c->a.nnx * c->a.nny, cudaMemcpyDeviceToHost));
   return CUPIC_OK;
 }
@@ -1411,7 +1619,7 @@ int cupic_get_phi(cupic_ctx *c, double *phi) {
   if (!c || !phi) return CUPIC_ERR_ARG;
   if (c->phi64) {  // the precision form's FP64 potential
     CU(cudaSetDevice(c->device));
-    CU(cudaStreamSynchronize(c->stream));
+    SETTLE(c);
     CU(cudaMemcpy(phi, c->phi64, sizeof(double) * c->a.nnx * c->a.nny, cudaMemcpyDeviceToHost));
     return CUPIC_OK;
   }
@@ -1425,14 +1633,14 @@ int cupic_get_phi(cupic_ctx *c, double *phi) {
 int cupic_set_phi(cupic_ctx *c, const double *phi) {
   if (!c || !phi) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
-  CU(cudaStreamSynchronize(c->stream));
+  SETTLE(c);
   return set_phi_both(c, phi);
 }
 
 int cupic_get_field_f32(cupic_ctx *c, float *ex, float *ey) {
   if (!c || !ex || !ey) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
-  CU(cudaStreamSynchronize(c->stream));
+  SETTLE(c);
   const size_t nodes = (size_t)c->a.nnx * c->a.nny;
   std::vector<float2> h(nodes);
   CU(cudaMemcpy(h.data(), c->a.E, nodes * sizeof(float2), cudaMemcpyDeviceToHost));
@@ -1460,7 +1668,7 @@ int cupic_get_stats(cupic_ctx *c, cupic_step_stats *out, int32_t count) {
   if (!c || !out || count < 0 || count > kStatsRing) return CUPIC_ERR_ARG;
   if (count == 0) return CUPIC_OK;
   CU(cudaSetDevice(c->device));
-  CU(cudaStreamSynchronize(c->stream));
+  SETTLE(c);
   int64_t step = 0;
   CU(cudaMemcpy(&step, &c->ctl->step, sizeof(step), cudaMemcpyDeviceToHost));
   // the ring entries of steps step-count .. step-1, in at most two copies
@@ -1498,7 +1706,7 @@ int cupic_density_profile(cupic_ctx *c, int species, double *density) {
 int cupic_get_flags(cupic_ctx *c, uint32_t *flags) {
   if (!c || !flags) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
-  CU(cudaStreamSynchronize(c->stream));
+  SETTLE(c);
   return read_ctl_flags(c, flags);
 }
 
@@ -1512,7 +1720,7 @@ int cupic_test_bounded_wait(cupic_ctx *c) {
 int cupic_clear_flags(cupic_ctx *c) {
   if (!c) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
-  CU(cudaStreamSynchronize(c->stream));
+  SETTLE(c);
   uint32_t z[2] = {0u, 0u};
   int32_t zero = 0;
   CU(cudaMemcpy(&c->ctl->flags, z, sizeof(z), cudaMemcpyHostToDevice));

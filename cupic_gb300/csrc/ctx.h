@@ -46,6 +46,9 @@ struct cupic_ctx {
   bool initialized = false;
   bool rho_valid = false;
   int host_cur = 0;
+  // advanced whenever rows or staging rows move to new buffers (a batch
+  // holding this context's SimArgs rebuilds)
+  int layout_epoch = 0;
 };
 
 // status helpers of capi.cu used by batch.cu

@@ -35,6 +35,8 @@ struct Ctl {
   unsigned long long absorbed[2];
   unsigned long long removed[2];
   int32_t abort;          // a bounded wait gave up: kernels bail out
+  int32_t halt;           // a row cannot take the step's arrivals: the rest of the run is idle
+  int32_t skipped;        // steps whose bookkeeping found the run halted (the halted one included)
   uint32_t jepoch;        // solves run so far: the base of the halo words' epochs
   uint32_t idle;          // never written: the bounded-wait self-test waits on it
   int32_t refine_done;    // precision-form solve: the stop test passed, later corrections idle
@@ -108,6 +110,14 @@ struct JacobiArgs {
 struct JGroup {
   int32_t first, G, begin, end;
 };
+
+// Set by the room check of a step whose arrivals do not fit their rows; the
+// host grows those rows and completes the step.  Every kernel of a step
+// reads it first and returns when it is set: the flag changes only between
+// kernels, so the whole grid sees one value.
+__device__ __forceinline__ bool halted(const Ctl *ctl) {
+  return *reinterpret_cast<const volatile int32_t *>(&ctl->halt) != 0;
+}
 
 // ---------------------------------------------------------------------------
 // arithmetic shared by the kernels

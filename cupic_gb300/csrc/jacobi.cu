@@ -306,7 +306,8 @@ template <int R>
 __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &J, const int c, float *jsm,
                                             float *red, int *bail_p) {
   int &bail = *bail_p;
-  if (J.gated && *reinterpret_cast<volatile int *>(&a.ctl->refine_done)) return;  // uniform: a flag of an earlier kernel
+  // uniform: flags of earlier kernels
+  if (halted(a.ctl) || (J.gated && *reinterpret_cast<volatile int *>(&a.ctl->refine_done))) return;
   const int G = J.G, tid = threadIdx.x;
   const int nnx = a.nnx, nny = a.nny, P = J.pitch;
   const int M = nny - 2;

@@ -18,6 +18,11 @@ cudaError_t launch_inject(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_inject_draw(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_inject_append(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_finalize(const SimArgs &a, cudaStream_t st);
+// room check between the push and the arrivals (sets ctl->halt), and the
+// move of a species' rows into a larger layout
+cudaError_t launch_room(const SimArgs &a, cudaStream_t st);
+cudaError_t launch_move_rows(const float4 *old, const int64_t *oseg, float4 *parts, const int64_t *nseg,
+                             const int32_t *keep, int ncy, cudaStream_t st);
 size_t push_smem_bytes(int nnx, int pb = 256);  // pb: threads per block (256 single context)
 cudaError_t push_set_smem(size_t bytes);
 // set-up on the context's stream
@@ -51,6 +56,7 @@ cudaError_t launch_push_deposit_batch(const SimArgs *inst, const int2 *row_work,
 cudaError_t launch_arrive_batch(const SimArgs *inst, const int2 *row_work, int n, cudaStream_t st);
 cudaError_t launch_inject_draw_batch(const SimArgs *inst, int n, int max_inj_cap, cudaStream_t st);
 cudaError_t launch_inject_append_batch(const SimArgs *inst, int n, int max_ncy, cudaStream_t st);
+cudaError_t launch_room_batch(const SimArgs *inst, int n, int max_ncy, cudaStream_t st);
 cudaError_t launch_finalize_batch(const SimArgs *inst, int n, cudaStream_t st);
 
 // fault-detection self-test (jacobi.cu)

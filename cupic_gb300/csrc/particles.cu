@@ -263,6 +263,7 @@ __global__ void k_linear_phi(SimArgs a, double phi_p, double *phi64) {
 
 // zero the accumulator the next deposit writes (rho[cur^1])
 __global__ void k_zero_next_rho(SimArgs a) {
+  if (halted(a.ctl)) return;
   unsigned long long *r = a.rho[a.ctl->cur ^ 1];
   const size_t n = (size_t)a.nnx * a.nny;
   for (size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x; k < n;
@@ -335,6 +336,7 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
   constexpr int CH = PB * kPPT;  // particles per chunk
   constexpr int NE = kPPT * NW;  // scan entries per chunk, (j, warp) in j-major order
   static_assert(NE <= 32, "one warp scans a chunk's entries");
+  if (halted(a.ctl)) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nnx = a.nnx;
   const int ncx = a.ncx;
@@ -509,6 +511,7 @@ __global__ void __launch_bounds__(PB, PB == 128 ? 8 : (PB == 256 ? 4 : 2))
 // append the movers: row d = [stayed] + [up from d-1] + [down from d+1]
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void arrive_row(const SimArgs &a, const int d, const int sp) {
+  if (halted(a.ctl)) return;
   const SpeciesDev &S = a.sp[sp];
   const int ns = S.nstay[d];
   const int nb = d > 0 ? S.nup[d - 1] : 0;
@@ -544,6 +547,7 @@ __global__ void __launch_bounds__(32 * kArriveWarps)
   if (t >= ntask) return;
   const int2 w = work[t >> 1];
   const SimArgs &a = inst[w.x];
+  if (halted(a.ctl)) return;
   const int d = w.y, sp = t & 1;
   const SpeciesDev &S = a.sp[sp];
   const int ns = S.nstay[d];
@@ -569,6 +573,64 @@ __global__ void __launch_bounds__(32 * kArriveWarps)
 }
 
 // ---------------------------------------------------------------------------
+// room check, between the push and the arrivals.  The reference reallocates
+// its particle array at every boundary call (cc.cu:195,260), so it never
+// runs out of room; here rows have fixed capacities.  Row d must take its
+// stayers, the movers staged for it from rows d-1 and d+1 and the particles
+// injected into it.  When one row of a species cannot, the run halts before
+// any particle is written: the later kernels of the step and of the steps
+// after it return at once, and the host grows the rows that are short,
+// completes the step and runs the steps that were skipped.  Nothing waits for
+// the host on the way, and the results are those of a run with larger rows.
+// It only reads and sets the flag, so it does not read the flag itself.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void room_check(const SimArgs &a, const int sp, int *inj) {
+  Ctl *ctl = a.ctl;
+  const SpeciesDev &S = a.sp[sp];
+  const int ncy = a.ncy;
+  for (int k = threadIdx.x; k < ncy; k += blockDim.x) inj[k] = 0;
+  __syncthreads();
+  const int ne = ctl->inj_gen[sp];
+  for (int k = threadIdx.x; k < ne; k += blockDim.x) {
+    const int d = S.inj_d[k];
+    if (d >= 0 && d < ncy) atomicAdd(&inj[d], 1);
+  }
+  __syncthreads();
+  int over = 0;
+  for (int d = threadIdx.x; d < ncy; d += blockDim.x) {
+    const long long need = (long long)S.nstay[d] + (d > 0 ? S.nup[d - 1] : 0) +
+                           (d + 1 < ncy ? S.ndown[d + 1] : 0) + inj[d];
+    over |= need > (long long)S.cap[d];
+  }
+  if (__syncthreads_or(over) && threadIdx.x == 0) atomicExch(&ctl->halt, 1);
+}
+
+constexpr int kRoomBlock = 512;
+
+__global__ void __launch_bounds__(kRoomBlock) k_room(SimArgs a) {
+  extern __shared__ int inj_rows[];
+  room_check(a, blockIdx.x, inj_rows);
+}
+
+// grid (species, instance)
+__global__ void __launch_bounds__(kRoomBlock) k_room_batch(const SimArgs *__restrict__ inst) {
+  extern __shared__ int inj_rows[];
+  room_check(inst[blockIdx.y], blockIdx.x, inj_rows);
+}
+
+// a species moved to a larger layout: the first keep[j] particles of row j
+// from old + oseg[j] to parts + nseg[j], in order (one block per row)
+__global__ void k_move_rows(const float4 *__restrict__ old, const int64_t *__restrict__ oseg,
+                            float4 *__restrict__ parts, const int64_t *__restrict__ nseg,
+                            const int32_t *__restrict__ keep) {
+  const int j = blockIdx.x;
+  const int n = keep[j];
+  const float4 *src = old + oseg[j];
+  float4 *dst = parts + nseg[j];
+  for (int k = threadIdx.x; k < n; k += blockDim.x) dst[k] = src[k];
+}
+
+// ---------------------------------------------------------------------------
 // injection of the half-Maxwellian flux at y = Ly (cc.cu:179-256), in three
 // kernels:
 //   k_inject_sched   the step's count and the injection time of every draw,
@@ -582,6 +644,7 @@ __global__ void __launch_bounds__(32 * kArriveWarps)
 __device__ __forceinline__ void inject_sched(const SimArgs &a, const int sp) {
   const SpeciesDev &S = a.sp[sp];
   Ctl *ctl = a.ctl;
+  if (halted(ctl)) return;
   const double t = ctl->t;
   const double fpt = t + a.dt_d;
   if (!ctl->tin_set[sp]) {
@@ -614,6 +677,7 @@ __global__ void k_inject_sched_batch(const SimArgs *__restrict__ inst, int n) {
 
 __device__ __forceinline__ void inject_gen(const SimArgs &a, const int sp, const int k) {
   const Ctl *ctl = a.ctl;
+  if (halted(ctl)) return;
   const int ne = ctl->inj_gen[sp];
   if (k >= ne) return;
   const SpeciesDev &S = a.sp[sp];
@@ -663,6 +727,7 @@ __device__ __forceinline__ void inject_append(const SimArgs &a, const int sp, in
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const SpeciesDev &S = a.sp[sp];
   Ctl *ctl = a.ctl;
+  if (halted(ctl)) return;
   __shared__ unsigned s_rem;
   if (tid == 0) s_rem = 0;
   for (int k = tid; k < a.ncy; k += kInjBlock) running[k] = 0;
@@ -736,6 +801,10 @@ __global__ void __launch_bounds__(kInjBlock) k_inject_append_batch(const SimArgs
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void finalize(const SimArgs &a) {
   Ctl *ctl = a.ctl;
+  if (halted(ctl)) {  // the host completes the halted step and reruns the ones counted here
+    if (threadIdx.x == 0) ctl->skipped += 1;
+    return;
+  }
   __shared__ unsigned long long live[2];
   if (threadIdx.x < 2) live[threadIdx.x] = 0ull;
   __syncthreads();
@@ -924,6 +993,22 @@ cudaError_t launch_inject_draw_batch(const SimArgs *inst, int n, int max_inj_cap
 
 cudaError_t launch_inject_append_batch(const SimArgs *inst, int n, int max_ncy, cudaStream_t st) {
   k_inject_append_batch<<<dim3(2, n), kInjBlock, max_ncy * sizeof(int), st>>>(inst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_room(const SimArgs &a, cudaStream_t st) {
+  k_room<<<2, kRoomBlock, a.ncy * sizeof(int), st>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_room_batch(const SimArgs *inst, int n, int max_ncy, cudaStream_t st) {
+  k_room_batch<<<dim3(2, n), kRoomBlock, max_ncy * sizeof(int), st>>>(inst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_move_rows(const float4 *old, const int64_t *oseg, float4 *parts, const int64_t *nseg,
+                             const int32_t *keep, int ncy, cudaStream_t st) {
+  k_move_rows<<<ncy, 256, 0, st>>>(old, oseg, parts, nseg, keep);
   return cudaGetLastError();
 }
 

@@ -30,6 +30,7 @@ __device__ __forceinline__ double source64(const SimArgs &a, const long long *ac
 
 // the FP64 source of every node, once per solve (0 on the Dirichlet rows)
 __global__ void __launch_bounds__(kRBlock) k_r64_source(SimArgs a, double *b64) {
+  if (halted(a.ctl)) return;
   const int j = blockIdx.y, nnx = a.nnx, nny = a.nny;
   const size_t rb = (size_t)j * nnx;
   const long long *acc = reinterpret_cast<const long long *>(a.rho[a.ctl->cur]);
@@ -41,7 +42,7 @@ __global__ void __launch_bounds__(kRBlock) k_r64_source(SimArgs a, double *b64) 
 // the bits of a non-negative double)
 __global__ void __launch_bounds__(kRBlock) k_r64_residual(SimArgs a, const double *phi64, const double *b64,
                                                          float *rr, unsigned long long *maxr, int gated) {
-  if (gated && *reinterpret_cast<volatile int *>(&a.ctl->refine_done)) return;
+  if (halted(a.ctl) || (gated && *reinterpret_cast<volatile int *>(&a.ctl->refine_done))) return;
   const int j = blockIdx.y, nnx = a.nnx, nny = a.nny;
   const size_t rb = (size_t)j * nnx;
   double m = 0.0;
@@ -73,7 +74,7 @@ __global__ void __launch_bounds__(kRBlock) k_r64_residual(SimArgs a, const doubl
 // phi64 += dl on interior rows (the FP32 potential follows once, at the end
 // of the solve)
 __global__ void __launch_bounds__(kRBlock) k_r64_update(SimArgs a, double *phi64, const float *dl, int gated) {
-  if (gated && *reinterpret_cast<volatile int *>(&a.ctl->refine_done)) return;
+  if (halted(a.ctl) || (gated && *reinterpret_cast<volatile int *>(&a.ctl->refine_done))) return;
   const int j = blockIdx.y, nnx = a.nnx;
   if (j < 1 || j > a.nny - 2) return;
   const size_t rb = (size_t)j * nnx;
@@ -83,6 +84,7 @@ __global__ void __launch_bounds__(kRBlock) k_r64_update(SimArgs a, double *phi64
 
 // the FP32 potential from phi64, at the end of a solve
 __global__ void __launch_bounds__(kRBlock) k_r64_phi32(SimArgs a, const double *phi64) {
+  if (halted(a.ctl)) return;
   const size_t rb = (size_t)blockIdx.y * a.nnx;
   for (int i = blockIdx.x * kRBlock + threadIdx.x; i < a.nnx; i += gridDim.x * kRBlock)
     a.phi[rb + i] = __double2float_rn(phi64[rb + i]);
@@ -95,7 +97,7 @@ __global__ void __launch_bounds__(kRBlock) k_r64_phi32(SimArgs a, const double *
 // solve's sweeps and residual
 __global__ void k_r64_decide(Ctl *ctl, const unsigned long long *maxr, int sweeps, int mn, int mx,
                              double tol, int write_stats) {
-  if (ctl->refine_done) return;
+  if (ctl->refine_done || halted(ctl)) return;
   const double res = __longlong_as_double((long long)*maxr);
   if ((sweeps >= mn && res < tol) || sweeps >= mx) {
     ctl->refine_done = 1;
@@ -108,6 +110,7 @@ __global__ void k_r64_decide(Ctl *ctl, const unsigned long long *maxr, int sweep
 
 // E = -grad phi from phi64 (mesh.cu:413-468), rounded once to FP32
 __global__ void __launch_bounds__(kRBlock) k_r64_field(SimArgs a, const double *phi64) {
+  if (halted(a.ctl)) return;
   const int j = blockIdx.y, nnx = a.nnx, nny = a.nny;
   const size_t rb = (size_t)j * nnx;
   for (int i = blockIdx.x * kRBlock + threadIdx.x; i < nnx; i += gridDim.x * kRBlock) {

@@ -23,10 +23,10 @@ MEMBERS = [
 ]
 
 
-def make_all():
+def make_all(**extra):
     out = []
     for name, over in MEMBERS:
-        s = cg.Sim(cg.workload_params(name, **over))
+        s = cg.Sim(cg.workload_params(name, **over, **extra))
         s.init_plasma()
         out.append(s)
     return out
@@ -85,4 +85,33 @@ def test_membership_changes_between_steps(gpu_lib):
             ref.close()
     finally:
         for s in batched:
+            s.close()
+
+
+def test_members_whose_rows_fill_up(gpu_lib):
+    """Members without row slack halt alone when a row runs out of room;
+    the batch's sync grows their rows and completes their steps, the next
+    batched step runs on the new buffers, and every member still equals its
+    solo run."""
+    alone, batched = make_all(row_slack=0.0), make_all(row_slack=0.0)
+    caps = [(int(np.ceil(s.p.ppr)) + 7) // 8 * 8 + 64 for s in batched]
+    steps, tick = 24, 4
+    most = [0] * len(batched)
+    try:
+        for s in alone:
+            s.step(steps)
+        with cg.Batch(batched) as b:
+            for _ in range(steps // tick):
+                b.step(tick)
+                for k, m in enumerate(batched):
+                    most[k] = max(most[k], int(m.row_counts(0).max()), int(m.row_counts(1).max()))
+        for k, (a, m) in enumerate(zip(alone, batched)):
+            compare(a, m, f"member {k}")
+            assert a.stats(steps) == m.stats(steps), f"member {k} stats"
+            assert m.flags() == 0
+        # the 64x256 member (pushed from the work list) and the 256x1024 one
+        # (pushed by the single-context kernel) outgrow their rows
+        assert most[3] > caps[3] and most[4] > caps[4], (most, caps)
+    finally:
+        for s in alone + batched:
             s.close()

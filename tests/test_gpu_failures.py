@@ -15,7 +15,7 @@ import cupic_gb300 as cg
 
 pytestmark = pytest.mark.gpu
 
-CFL, CAPACITY, NONFINITE, TIMEOUT = 1, 2, 8, 16
+CFL, CAPACITY, STAGE, NONFINITE, TIMEOUT = 1, 2, 4, 8, 16
 
 
 def plasma(p, rng, rows, per_row, vy=0.0):
@@ -84,13 +84,27 @@ def test_nonfinite_particle_is_removed_and_flagged(tiny):
     recovers(sim, p, rng)
 
 
-def test_row_overflow_is_flagged(tiny):
+def test_full_row_grows_instead_of_overflowing(tiny):
+    """A row that cannot take its arrivals is grown by the room check and the
+    host before any particle is written: no particle is lost, no flag."""
     p, sim = tiny
     rng = np.random.default_rng(3)
     # row 10 full at its capacity; row 9 sends all its particles up into it
     cap = (int(math.ceil(p.ppr)) + 7) // 8 * 8 + 64
     e = np.concatenate([plasma(p, rng, [10], cap - 8), plasma(p, rng, [9], 40, vy=10.0)])
     sim.load(0, e)
+    sim.step(1)
+    assert sim.flags() == 0
+    rows = sim.row_counts(0)
+    assert rows[10] == cap - 8 + 40 and rows[9] == 0
+
+
+def test_staging_overflow_is_flagged(tiny):
+    p, sim = tiny
+    rng = np.random.default_rng(4)
+    # 200 particles of row 9 move up in one step; loading them gives row 9
+    # 264 places and the staging rows 136, so 64 movers find no staging slot
+    sim.load(0, plasma(p, rng, [9], 200, vy=10.0))
     assert stepped(sim) == 5  # CUPIC_ERR_CAPACITY
-    assert sim.flags() & CAPACITY
+    assert sim.flags() & STAGE
     recovers(sim, p, rng)

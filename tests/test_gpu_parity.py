@@ -249,3 +249,77 @@ def test_probe_current_and_density_diagnostics(gpu_lib):
         assert sim.probe_current(10) == pytest.approx(want, rel=0, abs=1e-12)
         rows = sim.row_counts(1)
         np.testing.assert_allclose(sim.density_profile(1), rows / (p.ncx * p.ds ** 3), rtol=1e-15)
+
+
+def row_capacity(p, slack):
+    """The capacity a row gets at initialisation: ppr * (1 + slack) + 64,
+    rounded up to a multiple of 8."""
+    return (int(np.ceil(p.ppr * (1.0 + slack))) + 7) // 8 * 8 + 64
+
+
+def most_in_a_row(sim):
+    return max(int(sim.row_counts(0).max()), int(sim.row_counts(1).max()))
+
+
+def test_full_rows_grow_and_match_oracle(make_pair):
+    """Rows without slack (ppr + 64 places) run out of room within a few
+    steps.  The room check halts the run before any particle is written,
+    the host grows the rows that are short and completes the steps, and
+    every step still gives the oracle's bits; runs of ten graph-launched
+    steps halt and resume several times."""
+    sim, ora = make_pair("small", row_slack=0.0)
+    cap0 = row_capacity(sim.p, 0.0)
+    sim.init_plasma()
+    ora.init_plasma()
+    most = 0
+    for _ in range(4):
+        sim.step(10)
+        ora.step(10)
+        g, o = sim.stats(1)[0], ora.stats()
+        for k in ("step", "absorbed", "removed", "injected", "live", "sweeps"):
+            assert g[k] == o[k], f"{k}: gpu {g[k]} oracle {o[k]} at step {o['step']}"
+        assert g["flags"] == 0
+        most = max(most, most_in_a_row(sim))
+    assert most > cap0, "no row outgrew its first capacity"
+    check_state(sim, ora)
+
+
+def test_stage_api_grows_full_rows(make_pair):
+    """The reference's main loop (main.cu:61-73) on rows without slack:
+    particle_mover and cc grow the rows that cannot take their arrivals or
+    injected particles before writing them."""
+    sim, ora = make_pair("small", row_slack=0.0)
+    cap0 = row_capacity(sim.p, 0.0)
+    sim.init_plasma()
+    ora.init_plasma()
+    most = 0
+    for _ in range(8):
+        t = ora.get_time()[1]
+        sim.charge_deposition()
+        ora.deposit()
+        sim.poisson_solver(1e-30, 40, 40, 1)
+        ora.solve(1e-30, 40, 40, 1)
+        sim.field_solver()
+        ora.field()
+        sim.particle_mover()
+        ora.push(0)
+        sim.cc(t)
+        ora.inject(t)
+        most = max(most, most_in_a_row(sim))
+    assert most > cap0, "no row outgrew its first capacity"
+    check_state(sim, ora)
+
+
+def test_long_run_of_the_64x256_workload(make_pair):
+    """640 steps of the 64x256 workload: its top electron row passes the
+    default capacity (1.5 ppr + 64) at step 629 and holds about 2200
+    electrons at step 640, and the run goes on with the oracle's bits."""
+    sim, ora = make_pair("small")
+    cap0 = row_capacity(sim.p, sim.p.row_slack)
+    sim.init_plasma()
+    ora.init_plasma()
+    sim.step(640)
+    ora.step(640)
+    assert sim.stats(1)[0]["flags"] == 0
+    check_state(sim, ora)
+    assert most_in_a_row(sim) > cap0
