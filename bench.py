@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--requests", type=int, default=32, help="serving: requests in the stream")
     ap.add_argument("--rate", type=float, default=100.0, help="serving: Poisson arrivals per second")
     ap.add_argument("--solve-steps", type=int, default=300, help="serving: steps per request")
+    ap.add_argument("--sweeps", type=int, default=200,
+                    help="batched and serving: Jacobi sweeps per step of every instance")
     ap.add_argument("--no-plain", action="store_true", help="batched: skip the one-at-a-time run")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -454,7 +456,7 @@ def run_batched(args, local):
     together, against the same instances stepped one at a time."""
     import cupic_gb300 as cg
     from cupic_gb300.params import bias_instances
-    ps = bias_instances(args.instances, seed=2, sweeps=200)
+    ps = bias_instances(args.instances, seed=2, sweeps=args.sweeps)
     sims = []
     for p in ps:
         s = cg.Sim(p, device=local)
@@ -490,7 +492,7 @@ def run_batched(args, local):
         "speedup_vs_plain": plain_s / batch_s, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"{n} instances: Nx in {{32,64,128,256}}, Ny=4Nx, 10-50 particles "
                                f"per cell per species, phi_p in [-10,2], mi/me=1836, Ti/Te=0.1, "
-                               f"200 Jacobi sweeps, seeds from 2",
+                               f"{args.sweeps} Jacobi sweeps, seeds from 2",
                    "particles": parts, "cells": sum(p.ncx * p.ncy for p in ps)},
         "clocks": clocks,
     }
@@ -507,7 +509,7 @@ def run_serving(args, local):
     import copy
     from cupic_gb300 import serve
     from cupic_gb300.params import bias_instances
-    ps = bias_instances(args.requests, seed=3, sweeps=200)
+    ps = bias_instances(args.requests, seed=3, sweeps=args.sweeps)
     t = serve.poisson_arrivals(args.requests, args.rate, seed=3)
     reqs = [serve.Request(k, p, float(t[k]), steps=args.solve_steps,
                           window=min(1000, args.solve_steps // 2)) for k, p in enumerate(ps)]
@@ -524,6 +526,7 @@ def run_serving(args, local):
         "results_identical_to_plain": same, "dtype": "f32", "data": "synthetic",
         "config": {"requests": args.requests, "rate_per_s": args.rate,
                    "steps_per_request": args.solve_steps, "window": reqs[0].window,
+                   "jacobi_sweeps_per_step": args.sweeps,
                    "sizes": "Nx in {32,64,128,256}, Ny=4Nx, 10-50 ppc, phi_p in [-10,2]",
                    "admission": "16 B per particle + 12 B per cell within 96 GiB"},
     }

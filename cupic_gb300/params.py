@@ -132,7 +132,16 @@ def bias_instances(n=256, seed=2, sweeps=200, sizes=(32, 64, 128, 256)):
     `sizes`, Ny = 4 Nx, ds = 0.5, particles per cell per species uniform in
     10..50, phi_p uniform in [-10, 2], mi/me = 1836, Ti/Te = 0.1,
     dt = 0.05, `sweeps` Jacobi sweeps per step.  Instance i has its own
-    generator seed."""
+    generator seed.
+
+    These runs do not stay stable for long.  A fixed number of Jacobi sweeps
+    per step does not converge the potential on these meshes, so it lags the
+    charge.  A global oscillation of the potential grows until the movers of
+    a row overflow their staging row or electrons cross two rows in a step.
+    With 200 sweeps this happened near step 400-540 in every instance of
+    seed 3 (the oracle shows the same).  With 2000 sweeps it happened near
+    step 545-685 in every instance of 256 rows or more; the 32x128 ones
+    lasted 2000 steps."""
     import numpy as np
     rng = np.random.default_rng(seed)
     out = []
