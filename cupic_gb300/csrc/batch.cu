@@ -6,8 +6,9 @@
 //   - the solves: one cooperative launch whose CTAs are split into groups;
 //     a group of G CTAs solves its list of instances one after another
 //     (instances that fit one CTA's shared memory get G = 1, larger ones the
-//     fewest CTAs that hold them), groups sized and filled by the members'
-//     mesh work (largest first onto the least-loaded group);
+//     fewest CTAs that hold them, or with few members up to their share of
+//     the CTAs), groups sized and filled by the members' mesh work (largest
+//     first onto the least-loaded group);
 //   - push, arrive and the charge clear: work lists of {instance, row};
 //     instances of 512 rows or more, which fill the GPU by themselves, are
 //     pushed by the single-context kernel on parallel graph branches;
@@ -105,6 +106,17 @@ struct Plan {
   size_t smem;
 };
 
+// the layout on G > 1 CTAs, if their shared memory holds it
+bool plan_on(const SimArgs &a, int G, long long rows_fit, Plan *out) {
+  const int M = a.nny - 2;
+  const int P = (a.nnx + 3) / 4 * 4;
+  const int B = (M + G - 1) / G;
+  const int K = std::min(kBatchDepth, M / G);
+  if (G < 2 || K < 1 || B + 2 * K > rows_fit) return false;
+  *out = {G, B, K, P, jacobi_smem_bytes(B, K, P)};
+  return true;
+}
+
 bool plan_instance(const SimArgs &a, long long rows_fit, Plan *out) {
   const int M = a.nny - 2;
   const int P = (a.nnx + 3) / 4 * 4;
@@ -112,14 +124,8 @@ bool plan_instance(const SimArgs &a, long long rows_fit, Plan *out) {
     *out = {1, M, 1, P, jacobi_smem_bytes(M, 1, P)};
     return true;
   }
-  for (int G = 2; G <= M; ++G) {
-    const int B = (M + G - 1) / G;
-    const int K = std::min(kBatchDepth, M / G);
-    if (K >= 1 && B + 2 * K <= rows_fit) {
-      *out = {G, B, K, P, jacobi_smem_bytes(B, K, P)};
-      return true;
-    }
-  }
+  for (int G = 2; G <= M; ++G)
+    if (plan_on(a, G, rows_fit, out)) return true;
   return false;
 }
 
@@ -134,6 +140,7 @@ int build(cupic_batch *b) {
   std::vector<SimArgs> inst(n);
   std::vector<Plan> plan(n);
   std::vector<double> work(n);
+  std::vector<long long> fit(n);
   size_t smem = 0;
   b->max_nnx = b->max_ncy = b->max_inj = 0;
   for (int i = 0; i < n; ++i) {
@@ -141,6 +148,7 @@ int build(cupic_batch *b) {
     inst[i] = c->a;
     const long long P = (c->a.nnx + 3) / 4 * 4;
     const long long rows_fit = (long long)((dev_max - 1024) / (3 * sizeof(float) * P));
+    fit[i] = rows_fit;
     if (!plan_instance(c->a, rows_fit, &plan[i])) return CUPIC_ERR_ARG;
     smem = std::max(smem, plan[i].smem);
     work[i] = (double)c->a.nnx * c->a.nny * std::max(c->p.max_sweeps, 1);
@@ -152,6 +160,17 @@ int build(cupic_batch *b) {
   int per_sm = 0;
   CU(jacobi_batch_max_ctas(smem, &per_sm));
   const int T = per_sm * b->num_sms;
+  // With few members the fewest CTAs that hold a mesh leave most of the GPU
+  // idle: a member takes up to its share of the CTAs by work, but no more
+  // than its own tuned single-context layout.  More CTAs hold fewer rows
+  // each, so the shared memory per CTA does not grow.
+  const double wsum = std::accumulate(work.begin(), work.end(), 0.0);
+  for (int i = 0; i < n; ++i) {
+    const int share = (int)(T * work[i] / wsum);
+    const int want = std::min(b->members[i]->jG, share);
+    Plan q;
+    if (want > plan[i].G && plan_on(inst[i], want, fit[i], &q) && q.smem <= smem) plan[i] = q;
+  }
   // buckets of equal CTA count; groups per bucket by work share
   std::vector<int> sizes;
   for (const Plan &q : plan) sizes.push_back(q.G);
