@@ -40,7 +40,8 @@ enum {
   CUPIC_ERR_CUDA = 2,       /* a CUDA runtime call failed */
   CUPIC_ERR_NOMEM = 3,      /* device or host allocation failed */
   CUPIC_ERR_IO = 4,         /* input_data / particle file could not be read */
-  CUPIC_ERR_CAPACITY = 5,   /* a row or staging buffer would overflow */
+  CUPIC_ERR_CAPACITY = 5,   /* a staging row or the injection buffer overflowed (full
+                               rows are grown, not reported) */
   CUPIC_ERR_CFL = 6,        /* a particle moved more than one cell row in a step */
   CUPIC_ERR_NONFINITE = 7,  /* a NaN/Inf particle coordinate was seen */
   CUPIC_ERR_STATE = 8,      /* call out of order (e.g. step before init) */
@@ -90,7 +91,9 @@ typedef struct cupic_params {
   /* particles per y row per species at t=0: int(n*Lx*ds*ds) (init.cu:136) */
   int32_t ppr;
   /* storage: row capacity = ceil(ppr*(1+row_slack)) + 64; movers staged per
-   * row up to ceil(capacity*stage_frac) + 64 */
+   * row up to ceil(capacity*stage_frac) + 64.  A row that cannot take a
+   * step's particles is grown to ceil(need*(1+row_slack)) + 64 (and the
+   * staging rows with the largest row) before any particle is written. */
   double row_slack;
   double stage_frac;
   /* seed of the counter-based generator (Philox4x32-10) used for the
@@ -193,16 +196,21 @@ int cupic_poisson_solver(struct cupic_ctx *ctx, double max_error, int32_t min_sw
                          int32_t max_sweeps, int32_t check_every);
 int cupic_field_solver(struct cupic_ctx *ctx);
 /* Gather + leapfrog + periodic wrap + y-row binning + probe absorption;
- * also deposits the moved particles into the next charge accumulator. */
+ * also deposits the moved particles into the next charge accumulator.
+ * Rows that cannot take their arrivals are grown first. */
 int cupic_particle_mover(struct cupic_ctx *ctx);
 /* Injection of the half-Maxwellian flux at y=Ly for the step at time t and
  * end-of-step bookkeeping (cc.cu:134-272). */
 int cupic_cc(struct cupic_ctx *ctx, double t);
 
 /* nsteps full cycles (solve, field, push, bin, absorb, inject) with the
- * clock advancing by dt per step, replayed from a captured CUDA graph. */
+ * clock advancing by dt per step, replayed from a captured CUDA graph.
+ * Returns once the steps are enqueued.  A step whose particles do not fit
+ * their rows (checked on the device after the push) idles the rest of the
+ * run; the next call that waits grows those rows, completes that step and
+ * runs the remaining ones, with the results of a run with larger rows. */
 int cupic_step(struct cupic_ctx *ctx, int32_t nsteps);
-/* Waits for all work of ctx. */
+/* Waits for all work of ctx, completing a run that stopped for room. */
 int cupic_sync(struct cupic_ctx *ctx);
 
 /* Phases of a step, for cupic_step_timed. */
@@ -210,10 +218,10 @@ enum {
   CUPIC_PHASE_SOLVE = 0,  /* Jacobi sweeps + field (mesh.cu:55-154) */
   CUPIC_PHASE_ZERO = 1,   /* clearing the next charge accumulator (mesh.cu:35) */
   CUPIC_PHASE_PUSH = 2,   /* push + wrap + binning + deposition (particles.cu, cc.cu, mesh.cu) */
-  CUPIC_PHASE_ARRIVE = 3, /* movers appended to their new rows (cc.cu:640-772) */
-  CUPIC_PHASE_INJECT = 4, /* injected flux (cc.cu:134-272): the draws run on a side stream
-                             beside the push; this phase is the wait for them plus the
-                             append of the injected particles */
+  CUPIC_PHASE_ARRIVE = 3, /* movers appended to their new rows (cc.cu:640-772); the draws
+                             of the injected flux run on a side stream beside the push,
+                             and this phase includes the wait for them and the room check */
+  CUPIC_PHASE_INJECT = 4, /* append of the injected particles (cc.cu:134-272) */
   CUPIC_PHASE_FINAL = 5,  /* per-step counters and clock */
   CUPIC_NPHASE = 6
 };
