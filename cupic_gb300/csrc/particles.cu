@@ -582,7 +582,8 @@ __global__ void __launch_bounds__(32 * kArriveWarps)
 // after it return at once, and the host grows the rows that are short,
 // completes the step and runs the steps that were skipped.  Nothing waits for
 // the host on the way, and the results are those of a run with larger rows.
-// It only reads and sets the flag, so it does not read the flag itself.
+// The check writes nothing but the flag, so it runs in a halted run too
+// (it then finds the same rows short again) and needs no gate.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void room_check(const SimArgs &a, const int sp, int *inj) {
   Ctl *ctl = a.ctl;
