@@ -205,6 +205,7 @@ int layout_species(cupic_ctx *c, int sp, const std::vector<int32_t> &capv) {
     CU(cudaDeviceSynchronize());
   }
   destroy_graph(c);
+  ++c->layout_epoch;  // a batch holding this context's SimArgs rebuilds
   return CUPIC_OK;
 }
 
