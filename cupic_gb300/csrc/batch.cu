@@ -429,15 +429,23 @@ int cupic_batch_step(cupic_batch *b, int32_t nsteps) {
   if (!b || nsteps < 0) return CUPIC_ERR_ARG;
   if (b->members.empty() || nsteps == 0) return CUPIC_OK;
   CU(cudaSetDevice(b->device));
-  // a member whose rows grew (its run halted and was completed alone) has
-  // new buffers
-  for (size_t i = 0; i < b->members.size(); ++i)
-    if (b->members[i]->layout_epoch != b->epochs[i]) {
-      CU(cudaStreamSynchronize(b->stream));
-      const int rc = build(b);
+  // a member whose rows grew (its run halted and was completed alone) or
+  // whose particles were reloaded has new buffers; a reloaded one also needs
+  // the charge of its new particles
+  bool rebuild = false;
+  for (size_t i = 0; i < b->members.size(); ++i) {
+    cupic_ctx *c = b->members[i];
+    if (!c->rho_valid) {
+      const int rc = cupic_charge_deposition(c);
       if (rc) return rc;
-      break;
     }
+    if (c->layout_epoch != b->epochs[i]) rebuild = true;
+  }
+  if (rebuild) {
+    CU(cudaStreamSynchronize(b->stream));
+    const int rc = build(b);
+    if (rc) return rc;
+  }
   if (!b->graph_ok) {
     int rc = capture(b);
     if (rc) return rc;

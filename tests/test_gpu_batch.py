@@ -115,3 +115,32 @@ def test_members_whose_rows_fill_up(gpu_lib):
     finally:
         for s in alone + batched:
             s.close()
+
+
+def test_member_reloaded_between_steps(gpu_lib):
+    """A member whose electrons are reloaded between batched steps, with rows
+    fuller than their capacity (so they are laid out anew): the next batched
+    step deposits its charge, takes its new buffers, and it still equals its
+    solo run."""
+    alone, batched = make_all(), make_all()
+    try:
+        for s in alone:
+            s.step(2)
+        with cg.Batch(batched) as b:
+            b.step(2)
+            for s in (alone[2], batched[2]):
+                e = s.particles(0)
+                rows = np.floor(e[:, 1] / s.p.ds).astype(int)
+                extra = e[rows == rows.max()]
+                extra = np.concatenate([extra] * 3)  # the top row three times over
+                s.load(0, np.concatenate([e, extra]))
+            for s in alone:
+                s.step(3)
+            b.step(3)
+        for k, (a, m) in enumerate(zip(alone, batched)):
+            compare(a, m, f"member {k}")
+            assert a.stats(3) == m.stats(3), f"member {k} stats"
+            assert m.flags() == 0
+    finally:
+        for s in alone + batched:
+            s.close()
