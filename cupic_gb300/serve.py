@@ -15,6 +15,9 @@ and they join the batch at the next tick.  A tick is one ``Batch.step`` of all m
 steps, never past a member's last step); members that finish leave the
 batch and free their footprint.  A member's result is bit-identical to the
 one it gets alone, because batched and solo steps compute the same thing.
+A request whose context reports an error (a device flag: a particle that
+crossed two rows, a full staging row, a non-finite coordinate) fails alone:
+it leaves with its error and the others run on.
 """
 import collections
 import dataclasses
@@ -22,7 +25,7 @@ import time
 
 import numpy as np
 
-from . import Batch, Sim, reserve
+from . import Batch, CupicError, Sim, reserve
 from .params import footprint_bytes
 
 
@@ -36,6 +39,7 @@ class Request:
     start: float = None     # admission time
     finish: float = None    # result time
     current: float = None   # mean net absorbed charge per step over the window
+    error: str = None       # why the request failed (it then has no current)
 
     @property
     def latency(self):
@@ -105,21 +109,34 @@ def serve_batched(requests, budget_bytes=96 << 30, max_slots=512, tick=50, devic
                 r.start = clock() - t0
                 joining.append([r, sim, 0])
                 used += fp
+            failed = []
             if stepping:
-                batch.sync()
+                try:
+                    batch.sync()
+                except CupicError:
+                    # every member was waited for; those with a device flag
+                    # leave with their error, the others ran their k steps
+                    failed = [a for a in active if a[1].flags()]
+                    if not failed:
+                        raise
                 for a in active:
                     a[2] += k
+                for r, sim, _ in failed:
+                    r.error = f"device flags {sim.flags():#x}"
+                    r.finish = clock() - t0
+                gone = {id(a) for a in failed}
+                active = [a for a in active if id(a) not in gone]
             done = [a for a in active if a[2] >= a[0].steps]
             for r, sim, _ in done:
                 r.current = probe_current(sim, r.window)
                 r.finish = clock() - t0
-            if done or joining:
+            if done or joining or failed:
                 for a in joining:
                     a[1].sync()  # its initialisation is complete before the batch uses it
                 active = [a for a in active if a[2] < a[0].steps] + joining
                 joining = []
                 batch.set([a[1] for a in active])
-            for r, sim, _ in done:
+            for r, sim, _ in done + failed:
                 sim.close()
                 used -= footprint_bytes(r.params)
             if not active and not queue and pending:
@@ -146,6 +163,10 @@ def serve_plain(requests, device=0, clock=time.perf_counter):
             sim.init_plasma()
             sim.step(r.steps)
             r.current = probe_current(sim, r.window)
+        except CupicError:
+            if not sim.flags():
+                raise
+            r.error = f"device flags {sim.flags():#x}"
         finally:
             sim.close()
         r.finish = clock() - t0
@@ -153,8 +174,12 @@ def serve_plain(requests, device=0, clock=time.perf_counter):
 
 
 def summary(requests):
-    lat = np.array([r.latency for r in requests])
+    """Solves/s and latency percentiles of the requests that succeeded; the
+    span runs from the first arrival to the last finish of any request."""
+    ok = [r for r in requests if r.error is None]
+    lat = np.array([r.latency for r in ok]) if ok else np.zeros(1)
     span = max(r.finish for r in requests) - min(r.arrival for r in requests)
-    return {"solves": len(requests), "seconds": span, "solves_per_s": len(requests) / span,
+    return {"solves": len(ok), "failed": len(requests) - len(ok), "seconds": span,
+            "solves_per_s": len(ok) / span,
             "p50_ms": 1e3 * float(np.percentile(lat, 50)),
             "p99_ms": 1e3 * float(np.percentile(lat, 99))}

@@ -33,3 +33,21 @@ def test_each_result_is_the_same_alone_and_in_the_mix(gpu_lib, budget_fraction):
         assert m.finish >= m.start >= m.arrival
     s = serve.summary(mixed)
     assert s["solves"] == len(reqs) and s["p99_ms"] >= s["p50_ms"] > 0
+
+
+def test_a_failing_request_leaves_alone(gpu_lib):
+    """A request whose electrons the probe drives across two rows in one
+    step (a bias of -5000 Te/e) fails with its device flag, in the batch and
+    alone; every other request gets the result it gets alone."""
+    reqs = requests()
+    bad = reqs[3]
+    bad.params.phi_p = -5000.0
+    mixed = serve.serve_batched(copy.deepcopy(reqs), tick=20)
+    alone = serve.serve_plain(copy.deepcopy(reqs))
+    for m, a in zip(sorted(mixed, key=lambda r: r.rid), sorted(alone, key=lambda r: r.rid)):
+        if m.rid == bad.rid:
+            assert m.error and a.error and m.current is None and a.current is None
+        else:
+            assert m.error is None and m.current == a.current, f"request {m.rid}"
+    s = serve.summary(mixed)
+    assert s["failed"] == 1 and s["solves"] == len(reqs) - 1
