@@ -14,7 +14,6 @@ cudaError_t launch_zero_next_rho(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_leapfrog_start(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_push_deposit(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_arrive(const SimArgs &a, cudaStream_t st);
-cudaError_t launch_inject(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_inject_draw(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_inject_append(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_finalize(const SimArgs &a, cudaStream_t st);

@@ -948,12 +948,6 @@ cudaError_t launch_inject_append(const SimArgs &a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-cudaError_t launch_inject(const SimArgs &a, cudaStream_t st) {
-  cudaError_t e = launch_inject_draw(a, st);
-  if (e != cudaSuccess) return e;
-  return launch_inject_append(a, st);
-}
-
 template <int PB>
 cudaError_t push_batch(const SimArgs *inst, const int2 *row_work, int n, int max_nnx, cudaStream_t st) {
   static size_t cur = 48 * 1024;  // the attribute only grows
