@@ -521,8 +521,8 @@ def run_serving(args, local):
     line = {
         "metric": "bias-point solves/s (continuous batching)", "value": sm["solves_per_s"],
         "unit": "solves/s", "n_gpus": 1, "higher_is_better": True,
-        "p50_ms": sm["p50_ms"], "p99_ms": sm["p99_ms"],
-        "plain": sp, "speedup_vs_plain": sm["solves_per_s"] / sp["solves_per_s"],
+        "p50_ms": sm["p50_ms"], "p99_ms": sm["p99_ms"], "failed": sm["failed"],
+        "plain": sp, "speedup_vs_plain": sm["solves_per_s"] / max(sp["solves_per_s"], 1e-30),
         "results_identical_to_plain": same, "dtype": "f32", "data": "synthetic",
         "config": {"requests": args.requests, "rate_per_s": args.rate,
                    "steps_per_request": args.solve_steps, "window": reqs[0].window,
