@@ -21,9 +21,24 @@
 
 using namespace cupic;
 
+cudaError_t cupic::raise_dyn_smem(const void *kernel, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, size_t> cur;
+  if (bytes <= 48 * 1024) return cudaSuccess;  // below the default limit
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t &have = cur[std::make_pair(kernel, dev)];
+  if (bytes <= have) return cudaSuccess;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (e == cudaSuccess) have = bytes;
+  return e;
+}
+
 namespace {
 
-#define CU(call)                                   \
+#define CU(call)                                 \
   do {                                             \
     cudaError_t e_ = (call);                       \
     if (e_ != cudaSuccess) return cuda_status(e_); \

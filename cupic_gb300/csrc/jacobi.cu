@@ -685,13 +685,8 @@ size_t jacobi_smem_bytes(int rows_per_cta, int depth, int pitch) {
   return (size_t)3 * (rows_per_cta + 2 * depth) * pitch * sizeof(float);
 }
 
-// the attribute only grows, so contexts of different sizes can coexist
 cudaError_t jacobi_set_smem(size_t bytes) {
-  static size_t cur = 0;
-  if (bytes <= cur) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(k_jacobi, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  if (e == cudaSuccess) cur = bytes;
-  return e;
+  return raise_dyn_smem(reinterpret_cast<const void *>(k_jacobi), bytes);
 }
 
 cudaError_t jacobi_max_ctas(size_t smem, int *per_sm) {
@@ -711,12 +706,7 @@ cudaError_t launch_wait_probe(const SimArgs &a, cudaStream_t st) {
 }
 
 cudaError_t jacobi_batch_set_smem(size_t bytes) {
-  static size_t cur = 48 * 1024;
-  if (bytes <= cur) return cudaSuccess;
-  cudaError_t e =
-      cudaFuncSetAttribute(k_jacobi_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  if (e == cudaSuccess) cur = bytes;
-  return e;
+  return raise_dyn_smem(reinterpret_cast<const void *>(k_jacobi_batch), bytes);
 }
 
 cudaError_t jacobi_batch_max_ctas(size_t smem, int *per_sm) {

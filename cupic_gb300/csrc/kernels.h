@@ -8,6 +8,12 @@
 
 namespace cupic {
 
+// Raises a kernel's dynamic shared memory limit on the current device to at
+// least `bytes`.  The attribute is per device, so the largest size set so
+// far is kept per (kernel, device), under a lock; it only grows, so
+// contexts of different sizes coexist.
+cudaError_t raise_dyn_smem(const void *kernel, size_t bytes);
+
 cudaError_t launch_init_particles(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_deposit(const SimArgs &a, cudaStream_t st);
 cudaError_t launch_zero_next_rho(const SimArgs &a, cudaStream_t st);

@@ -2,10 +2,13 @@
 // allocating any memory.
 //
 // Some callers cannot call cudaMalloc at the point where they need a solve:
-// - code running inside a CUDA stream capture;
-// - a real-time loop that forbids allocation after start-up;
-// - a host application whose device memory is all handed out by its own pool.
+// - a real-time loop that forbids allocation after start-up, because an
+//   allocation can block for an unbounded time;
+// - a host application whose device memory is all handed out by its own
+//   pool, so a cudaMalloc outside that pool would fail or fragment it.
 // They own the charge, potential and field buffers and just need the solve.
+// The call waits for its own work (it reads the sweep count and residual
+// back before returning).
 //
 // Such a call still needs scratch memory for the solver CTAs: per-CTA sweep
 // counters, residual slots, the halo rows they trade, and a small status
@@ -92,7 +95,9 @@ extern "C" int cupic_poisson_solver_static(const cupic_params *p, const int64_t 
   };
   // one CTA when the whole mesh fits; otherwise the most CTAs (up to one per
   // SM) for which some halo depth K >= 1 fits both the CTA's shared memory
-  // and the static scratch, with the deepest such K (at most 16)
+  // and the static scratch, with the deepest such K (at most 16).  The
+  // library-wide tuning variable CUPIC_JACOBI_CTAS, when set, caps the CTA
+  // count here as it does for a context's solve.
   const char *env = getenv("CUPIC_JACOBI_CTAS");
   const int forced = env ? atoi(env) : 0;
   int G = 0, B = 0, K = 0;

@@ -29,11 +29,11 @@ __device__ __forceinline__ void raise_flags(Ctl *ctl, uint32_t f) {
 }
 
 // Charge deposition into shared memory by cell moments.  A particle with
-// 16-bit fixed-point offsets FX, FY in [0, 65536] in its cell and cross term
-// FXY = round(FX*FY / 2^16) (cic_fixed) gives its four nodes the weights
-//   upper-right w11 = 2^16 FXY,          lower-right w10 = 2^16 FX - w11,
-//   upper-left  w01 = 2^16 FY - w11,     lower-left  w00 = 2^32 - 2^16 (FX + FY) + w11,
-// the CIC weights with FX*FY rounded to a multiple of 2^16; they sum to 2^32.
+// fixed-point offsets FX, FY in [0, 2^18] in its cell and cross term
+// FXY = round(FX*FY / 2^18) (cic_fixed) gives its four nodes the weights
+//   upper-right w11 = 2^14 FXY,          lower-right w10 = 2^14 FX - w11,
+//   upper-left  w01 = 2^14 FY - w11,     lower-left  w00 = 2^32 - 2^14 (FX + FY) + w11,
+// the CIC weights with FX*FY rounded to a multiple of 2^14; they sum to 2^32.
 // Over the particles of a cell the four node sums follow from four integer
 // moments M1 = count, MX = sum FX, MY = sum FY, MXY = sum FXY by the same
 // formulas.  Shared memory atomics are native for 32-bit integers only, so
@@ -45,7 +45,7 @@ __device__ __forceinline__ void raise_flags(Ctl *ctl, uint32_t f) {
 // global memory, that often and at every change of species.  Deposits
 // whose cell row is outside the tile go straight to global memory as int64
 // node weights.
-constexpr int kFoldParticles = 63 * 1024;  // 64512 * 65536 < 2^32
+constexpr int kFoldParticles = (1 << (32 - kFixBits)) - 1;  // 16383 * 2^18 < 2^32
 
 struct RhoMoments {
   unsigned *m;     // [4][ncr*ncx]: M1, MX, MY, MXY
@@ -79,7 +79,9 @@ struct RhoMoments {
   __device__ __forceinline__ long long m1(int c) const { return (long long)m[c]; }
   __device__ __forceinline__ long long mx(int c) const { return (long long)m[cells() + c]; }
   __device__ __forceinline__ long long my(int c) const { return (long long)m[2 * cells() + c]; }
-  __device__ __forceinline__ long long mxy(int c) const { return (long long)m[3 * cells() + c] << 16; }
+  __device__ __forceinline__ long long mxy(int c) const {
+    return (long long)m[3 * cells() + c] << kFixShift;
+  }
   // moments (of charge q particles) -> node sums added to global memory,
   // then clear the moments; callers __syncthreads() before, and before the
   // next deposit
@@ -89,15 +91,15 @@ struct RhoMoments {
       long long v = 0;
       if (i < ncx && j < ncr) {  // this node is the lower-left corner of cell (i, j)
         const int c = j * ncx + i;
-        v += m1(c) * 4294967296ll - 65536ll * (mx(c) + my(c)) + mxy(c);
+        v += m1(c) * 4294967296ll - ((mx(c) + my(c)) << kFixShift) + mxy(c);
       }
       if (i >= 1 && j < ncr) {  // lower-right corner of cell (i-1, j)
         const int c = j * ncx + i - 1;
-        v += 65536ll * mx(c) - mxy(c);
+        v += (mx(c) << kFixShift) - mxy(c);
       }
       if (i < ncx && j >= 1) {  // upper-left corner of cell (i, j-1)
         const int c = (j - 1) * ncx + i;
-        v += 65536ll * my(c) - mxy(c);
+        v += (my(c) << kFixShift) - mxy(c);
       }
       if (i >= 1 && j >= 1) {  // upper-right corner of cell (i-1, j-1)
         v += mxy((j - 1) * ncx + i - 1);
@@ -336,6 +338,8 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
   constexpr int CH = PB * kPPT;  // particles per chunk
   constexpr int NE = kPPT * NW;  // scan entries per chunk, (j, warp) in j-major order
   static_assert(NE <= 32, "one warp scans a chunk's entries");
+  constexpr int kCheckChunks = 8192 / CH;  // chunks between fold checks
+  static_assert((kCheckChunks + 1) * CH < kFoldParticles, "a fold check interval fits the moments");
   if (halted(a.ctl)) return;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nnx = a.nnx;
@@ -346,6 +350,7 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
   __shared__ __align__(8) uint64_t full[kStages];
   __shared__ uint2 wmask[2][NE];  // per-entry category ballots, alternate chunks
   __shared__ unsigned long long s_cnt[2];
+  __shared__ unsigned s_cmax[NW];  // per-warp largest cell count, at a fold check
 
   Ctl *ctl = a.ctl;
   const SpeciesDev &S = a.sp[sp];
@@ -367,7 +372,6 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
     }
   }
   RhoMoments T{tmom, s - 1, 3, ncx, nnx, a.nny, a.rho[ctl->cur ^ 1]};
-  int since_fold = 0;  // chunks deposited since the last fold
   T.zero();
   for (int k = tid; k < 2 * nnx; k += PB) etile[k] = a.E[(size_t)s * nnx + k];
   __syncthreads();
@@ -411,6 +415,15 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
       b1[j] = __ballot_sync(kFull, cat[j] & 2);
       if (lane == 0) wm[j * NW + warp] = make_uint2(b0[j], b1[j]);
     }
+    // fold check, every kCheckChunks chunks (block-uniform): the largest
+    // cell count so far, read while this chunk's deposits may still land
+    const bool check = (k % kCheckChunks) == kCheckChunks - 1 && k + 1 < nch;
+    if (check) {
+      unsigned c = 0u;
+      for (int i = tid; i < T.cells(); i += PB) c = max(c, T.m[i]);
+      c = __reduce_max_sync(kFull, c);
+      if (lane == 0) s_cmax[warp] = c;
+    }
     __syncthreads();  // the only block barrier of a chunk
     // every thread holds its particles: refill this stage with chunk k+kStages
     if (tid == 0 && k + kStages < nch) {
@@ -449,14 +462,22 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
     c_stay += (int)(field0(exl) + field0(vl));
     c_up += (int)(field1(exl) + field1(vl));
     c_dn += (int)(field2(exl) + field2(vl));
-    // fold before the moments could overflow (block-uniform); the barrier
-    // after it orders the clearing before the next chunk's deposits
-    ++since_fold;
-    if (k + 1 < nch && (since_fold + 1) * CH > kFoldParticles) {
-      __syncthreads();
-      T.fold(qc);
-      __syncthreads();
-      since_fold = 0;
+    // Fold before the moments could overflow.  A cell's moments stay below
+    // 2^32 while its count stays at most kFoldParticles.  The count read at
+    // the check misses at most this chunk's CH deposits, and the next check
+    // comes kCheckChunks chunks later, so without a fold no cell can pass
+    // cmax + (kCheckChunks + 1) * CH before then.  At ordinary densities
+    // that stays far below the limit and a row folds only at its end.  The
+    // barrier after a fold orders the clearing before the next deposits.
+    if (check) {
+      unsigned cmax = 0u;
+#pragma unroll
+      for (int w = 0; w < NW; ++w) cmax = max(cmax, s_cmax[w]);
+      if (cmax + (unsigned)((kCheckChunks + 1) * CH) > (unsigned)kFoldParticles) {
+        __syncthreads();
+        T.fold(qc);
+        __syncthreads();
+      }
     }
   }
   if (tid == 0) {
@@ -911,14 +932,8 @@ cudaError_t launch_leapfrog_start(const SimArgs &a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// the attribute only grows, so contexts of different sizes can coexist
 cudaError_t push_set_smem(size_t bytes) {
-  static size_t cur = 48 * 1024;
-  if (bytes <= cur) return cudaSuccess;
-  cudaError_t e =
-      cudaFuncSetAttribute(k_push_deposit, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-  if (e == cudaSuccess) cur = bytes;
-  return e;
+  return raise_dyn_smem(reinterpret_cast<const void *>(k_push_deposit), bytes);
 }
 
 cudaError_t launch_push_deposit(const SimArgs &a, cudaStream_t st) {
@@ -950,14 +965,9 @@ cudaError_t launch_inject_append(const SimArgs &a, cudaStream_t st) {
 
 template <int PB>
 cudaError_t push_batch(const SimArgs *inst, const int2 *row_work, int n, int max_nnx, cudaStream_t st) {
-  static size_t cur = 48 * 1024;  // the attribute only grows
   const size_t sm = push_smem_bytes(max_nnx, PB);
-  if (sm > cur) {
-    cudaError_t e = cudaFuncSetAttribute(k_push_deposit_batch<PB>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    cur = sm;
-  }
+  cudaError_t e = raise_dyn_smem(reinterpret_cast<const void *>(k_push_deposit_batch<PB>), sm);
+  if (e != cudaSuccess) return e;
   k_push_deposit_batch<PB><<<2 * n, PB, sm, st>>>(inst, row_work);
   return cudaGetLastError();
 }

@@ -274,14 +274,16 @@ int cupic_test_bounded_wait(struct cupic_ctx *ctx);
 
 /* The Poisson solve (and field) on caller-owned DEVICE buffers, allocating
  * nothing.  It has no counterpart in the reference.  It is for callers that
- * cannot call cudaMalloc: code inside a stream capture, real-time loops that
- * forbid allocation, hosts whose device memory comes from their own pool.
+ * cannot call cudaMalloc at solve time: real-time loops that forbid
+ * allocation after start-up (an allocation can block for an unbounded
+ * time), and hosts whose device memory all comes from their own pool.
  *   rho_dev  nnx*nny raw int64 fixed-point charge (2^32 per unit charge, the
  *            layout of cupic_get_rho_fixed, columns 0 and nnx-1 not folded)
  *   phi_dev  nnx*nny float potential, read as the initial guess, overwritten
  *   e_dev    nnx*nny {Ex, Ey} float pairs, written; NULL skips the field
  *   stream   a cudaStream_t, NULL for the default stream; the call waits for
- *            its own work before returning
+ *            its own work before returning (it reads sweeps_out and
+ *            residual_out back)
  * The solver's scratch (sweep counters, residual slots and the halo rows its
  * CTAs trade) lives in a static 8 MiB device array that every GPU loading
  * this library holds until exit.  The call lowers the halo depth, then the
@@ -291,7 +293,9 @@ int cupic_test_bounded_wait(struct cupic_ctx *ctx);
  * looks the array up (cudaGetSymbolAddress); make that first call before any
  * stream capture.  All calls share the array and it keeps the last call's
  * contents: calls that overlap on the GPU (other streams, other host
- * threads) race and must be serialised by the caller. */
+ * threads) race and must be serialised by the caller.  The environment
+ * variable CUPIC_JACOBI_CTAS, when set, caps the number of solver CTAs, as
+ * it does for a context's solve. */
 int cupic_poisson_solver_static(const cupic_params *p, const int64_t *rho_dev, float *phi_dev,
                                 float *e_dev, double max_error, int32_t min_sweeps,
                                 int32_t max_sweeps, int32_t check_every, void *stream,

@@ -59,6 +59,7 @@ def lib():
         L.ora_get_counts.argtypes = [vp, P(ctypes.c_int64), P(ctypes.c_int64)]
         L.ora_get_particles.argtypes = [vp, ctypes.c_int, P(ctypes.c_double)]
         L.ora_get_row_counts.argtypes = [vp, ctypes.c_int, P(ctypes.c_int32)]
+        L.ora_gather.argtypes = [vp, ctypes.c_int, P(ctypes.c_double), P(ctypes.c_double)]
         L.ora_get_phi.argtypes = [vp, P(ctypes.c_double)]
         L.ora_set_phi.argtypes = [vp, P(ctypes.c_double)]
         L.ora_get_field.argtypes = [vp, P(ctypes.c_double), P(ctypes.c_double)]
@@ -188,6 +189,15 @@ class Oracle:
         if n:
             _check(self.L.ora_get_particles(self.h, species, _dp(out)), "particles")
         return out
+
+    def gather(self, species):
+        """E interpolated at every particle of a species (the push's CIC
+        gather), in row order: (ex, ey)."""
+        n = self.counts()[species]
+        ex, ey = np.empty(n), np.empty(n)
+        if n:
+            _check(self.L.ora_gather(self.h, species, _dp(ex), _dp(ey)), "gather")
+        return ex, ey
 
     def row_counts(self, species):
         out = np.empty(self.p.ncy, dtype=np.int32)

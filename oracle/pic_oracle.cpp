@@ -269,15 +269,15 @@ struct Sim {
     const R fy = clamp01<R>(sy - (R)jc);
     const size_t n00 = (size_t)jc * nnx + ic;
     if constexpr (F32) {
-      /* CIC weights in 16-bit fixed point per axis, the cross term FX*FY
-       * rounded to a multiple of 2^16; the four sum to 2^32 */
-      const int64_t FX = (int64_t)std::rint(fx * 65536.0f);
-      const int64_t FY = (int64_t)std::rint(fy * 65536.0f);
-      const int64_t W11 = ((FX * FY + 32768) >> 16) << 16;
+      /* CIC weights in 18-bit fixed point per axis, the cross term FX*FY
+       * rounded to a multiple of 2^14; the four sum to 2^32 */
+      const int64_t FX = (int64_t)std::rint(fx * 262144.0f);
+      const int64_t FY = (int64_t)std::rint(fy * 262144.0f);
+      const int64_t W11 = ((FX * FY + 131072) >> 18) << 14;
       const int64_t qq = qs < 0 ? -1 : 1;
-      sink(n00, qq * ((int64_t)1 << 32) - qq * ((FX + FY) << 16) + qq * W11);
-      sink(n00 + 1, qq * ((FX << 16) - W11));
-      sink(n00 + nnx, qq * ((FY << 16) - W11));
+      sink(n00, qq * ((int64_t)1 << 32) - qq * ((FX + FY) << 14) + qq * W11);
+      sink(n00 + 1, qq * ((FX << 14) - W11));
+      sink(n00 + nnx, qq * ((FY << 14) - W11));
       sink(n00 + nnx + 1, qq * W11);
     } else {
       const double gx = 1.0 - fx, gy = 1.0 - fy;
@@ -1006,6 +1006,23 @@ int ora_get_particles(void *h, int sp, double *out) {
         out[k++] = (double)a.y;
         out[k++] = (double)a.vx;
         out[k++] = (double)a.vy;
+      }
+    return (int)CUPIC_OK;
+  });
+}
+
+/* the push's CIC field gather (particles.cu:145-180, D4 fixed) at every
+ * particle of a species, in row order */
+int ora_gather(void *h, int sp, double *ex, double *ey) {
+  if (sp < 0 || sp > 1 || !ex || !ey) return CUPIC_ERR_ARG;
+  return dispatch(h, [&](auto &s) {
+    size_t k = 0;
+    for (int r = 0; r < s.ncy; ++r)
+      for (const auto &a : s.rows[sp][r]) {
+        decltype(a.x) gx, gy;
+        s.gather(a, r, gx, gy);
+        ex[k] = (double)gx;
+        ey[k++] = (double)gy;
       }
     return (int)CUPIC_OK;
   });

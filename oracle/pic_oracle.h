@@ -49,6 +49,8 @@ int ora_step(void *h, int32_t nsteps);
 int ora_get_counts(void *h, int64_t *ne, int64_t *ni);
 int ora_get_particles(void *h, int species, double *xyvv);
 int ora_get_row_counts(void *h, int species, int32_t *counts);
+/* E at every particle of a species (the push's CIC gather), in row order */
+int ora_gather(void *h, int species, double *ex, double *ey);
 int ora_get_phi(void *h, double *phi);
 int ora_set_phi(void *h, const double *phi);
 int ora_get_field(void *h, double *ex, double *ey);

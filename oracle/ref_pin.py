@@ -1,6 +1,8 @@
 """Build and run the reference's own input_data getters (src/init.cu:424-789)
 and, in a second program, its particle-file reader and snapshot writers
-(src/init.cu:348-420, src/diagnostic.cu:48-215).
+(src/init.cu:348-420, src/diagnostic.cu:48-215); and compile the device
+code of its mesh and particle kernels (src/mesh.cu, src/particles.cu) into
+cubins that oracle/ref_kernels.py runs on a GPU.
 
 TEST INFRASTRUCTURE ONLY.  The reference's sources are compiled where they
 lie (REF_SRC below) with nvcc into oracle/_ref/ -- never copied -- together with:
@@ -9,7 +11,7 @@ lie (REF_SRC below) with nvcc into oracle/_ref/ -- never copied -- together with
   already defines (defect D1);
 - a harness (ref_pin/pin_main.cpp) that calls the getters and prints every
   derived parameter as exact hex doubles.
-No GPU is needed: only host functions run.
+The getters and file programs need no GPU: only host functions run.
 """
 import json
 import os
@@ -21,7 +23,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PIN = os.path.join(HERE, "ref_pin")
 OUT = os.path.join(HERE, "_ref")
 BIN = os.path.join(OUT, "ref_pin")
-REF_SRC = "/root/reference/src"
+# where the reference's sources lie; this recipe is the one place that names
+# it, and CUPIC_REFERENCE_SRC overrides it
+REF_SRC = os.environ.get("CUPIC_REFERENCE_SRC", "/root/reference/src")
 UNITS = ["init", "cc", "particles", "diagnostic", "cuda", "mesh"]
 
 
@@ -110,3 +114,32 @@ def run_files(workdir):
     os.makedirs(os.path.join(workdir, "run"), exist_ok=True)
     os.makedirs(os.path.join(workdir, "output"), exist_ok=True)
     subprocess.run([exe, workdir], check=True)
+
+
+# Device code of the reference's kernels, for tests/test_gpu_ref_kernels.py:
+# one cubin per source file, sm_103a, compiled with nvcc's default arithmetic
+# flags as the reference's own makefile does (src/makefile:6).  A cubin holds
+# GPU code only, so it runs on any host architecture through the driver API.
+KERNEL_CUBINS = {u: os.path.join(OUT, f"ref_{u}.cubin") for u in ("mesh", "particles")}
+
+
+def build_kernels(force=False):
+    """Compile oracle/_ref/ref_{mesh,particles}.cubin from the reference's
+    src/mesh.cu and src/particles.cu where they lie (mesh.cu with the D1
+    rename of its own double atomicAdd).  Returns the paths, or None when
+    the sources are absent."""
+    if not available():
+        return None
+    if all(os.path.exists(c) for c in KERNEL_CUBINS.values()) and not force:
+        return KERNEL_CUBINS
+    os.makedirs(OUT, exist_ok=True)
+    procs = []
+    for u, out in KERNEL_CUBINS.items():
+        extra = ["-include", os.path.join(PIN, "d1_guard.h")] if u == "mesh" else []
+        procs.append(subprocess.Popen(["nvcc", "-cubin", "-gencode", "arch=compute_103a,code=sm_103a",
+                                       "-I", PIN, "-w"] + extra +
+                                      [os.path.join(REF_SRC, u + ".cu"), "-o", out]))
+    for p in procs:
+        if p.wait() != 0:
+            raise RuntimeError("nvcc failed on a reference source")
+    return KERNEL_CUBINS

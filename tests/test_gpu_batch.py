@@ -9,6 +9,8 @@ import numpy as np
 import pytest
 
 import cupic_gb300 as cg
+from oracle.oracle import Oracle
+from parity import check_state, check_stats
 
 pytestmark = pytest.mark.gpu
 
@@ -143,4 +145,28 @@ def test_member_reloaded_between_steps(gpu_lib):
             assert m.flags() == 0
     finally:
         for s in alone + batched:
+            s.close()
+
+
+def test_batched_large_member_matches_oracle(gpu_lib):
+    """The 256x1024 member, solved by a group of CTAs inside the batched
+    launch and pushed by the batched kernels, equals the FP32 oracle bit for
+    bit (particles, rows, charge, potential, field, counters), not only its
+    own solo run."""
+    members = make_all()
+    big = members[4]
+    assert (big.p.ncx, big.p.ncy) == (256, 1024)
+    ora = Oracle(big.p, fp64=False)
+    ora.init_plasma()
+    try:
+        with cg.Batch(members) as b:
+            for _ in range(3):
+                b.step(1)
+                b.sync()
+                ora.step(1)
+                check_stats(big.stats(1)[0], ora.stats())
+        check_state(big, ora)
+    finally:
+        ora.close()
+        for s in members:
             s.close()

@@ -13,44 +13,9 @@ import pytest
 
 import cupic_gb300 as cg
 from oracle.oracle import Oracle
+from parity import check_state, check_stats
 
 pytestmark = pytest.mark.gpu
-
-RTOL = 1e-5  # contract tolerance for FP32 quantities
-
-
-def rel_err(g, o):
-    g = np.asarray(g, dtype=np.float64)
-    o = np.asarray(o, dtype=np.float64)
-    scale = max(np.abs(o).max(), 1e-30)
-    return float(np.abs(g - o).max() / scale) if g.size else 0.0
-
-
-def check_fp32(g, o, what):
-    assert g.shape == o.shape, f"{what}: shape {g.shape} vs {o.shape}"
-    err = rel_err(g, o)
-    assert err <= RTOL, f"{what}: relative error {err:.3e} > {RTOL}"
-    return err
-
-
-def check_state(sim, ora, exact=True):
-    for sp in (0, 1):
-        rg, ro = sim.row_counts(sp), ora.row_counts(sp)
-        np.testing.assert_array_equal(rg, ro, err_msg=f"row counts of species {sp}")
-        g, o = sim.particles(sp), ora.particles(sp)
-        check_fp32(g, o, f"particles of species {sp}")
-        if exact:
-            np.testing.assert_array_equal(g, o, err_msg=f"particles of species {sp} (bitwise)")
-    np.testing.assert_array_equal(sim.rho_fixed(0), ora.rho_fixed(), err_msg="fixed-point charge")
-    check_fp32(sim.phi(), ora.phi(), "phi")
-    exg, eyg = sim.efield()
-    exo, eyo = ora.efield()
-    check_fp32(exg, exo, "Ex")
-    check_fp32(eyg, eyo, "Ey")
-    if exact:
-        np.testing.assert_array_equal(sim.phi().astype(np.float64), ora.phi(), err_msg="phi bitwise")
-        np.testing.assert_array_equal(exg.astype(np.float64), exo, err_msg="Ex bitwise")
-        np.testing.assert_array_equal(eyg.astype(np.float64), eyo, err_msg="Ey bitwise")
 
 
 @pytest.fixture
@@ -93,8 +58,7 @@ def test_steps_match_oracle(make_pair, name, steps):
         ora.step(1)
         g = sim.stats(1)[0]
         o = ora.stats()
-        for k in ("step", "absorbed", "removed", "injected", "live", "sweeps"):
-            assert g[k] == o[k], f"{k}: gpu {g[k]} oracle {o[k]} at step {o['step']}"
+        check_stats(g, o)
         assert g["residual"] == pytest.approx(o["residual"], rel=0, abs=0)
         assert g["flags"] == 0
         gs.append(g)
@@ -323,3 +287,41 @@ def test_long_run_of_the_64x256_workload(make_pair):
     assert sim.stats(1)[0]["flags"] == 0
     check_state(sim, ora)
     assert most_in_a_row(sim) > cap0
+
+
+def test_dense_cell_folds_its_charge_moments(make_pair):
+    """40000 electrons in one cell, more than the 16383 a cell's 32-bit
+    charge moments hold before they must be folded into the int64
+    accumulator: the standalone deposit and the push's deposit both fold in
+    time and give the oracle's charge bit for bit."""
+    sim, ora = make_pair("tiny")
+    ora.init_plasma()
+    ora.step(1)
+    rng = np.random.default_rng(5)
+    n = 40000
+    dense = np.empty((n, 4))
+    dense[:, 0] = 2.0 + 0.5 * rng.random(n)      # cell column 4 (ds = 0.5)
+    dense[:, 1] = 2.5 + 0.5 * rng.random(n)      # cell row 5
+    dense[:, 2:] = 1e-3 * rng.standard_normal((n, 2))
+    dense = dense.astype(np.float32).astype(np.float64)
+    electrons = np.concatenate([ora.particles(0), dense])
+    ora.load(0, electrons)
+    for sp in (0, 1):
+        sim.load(sp, ora.particles(sp))
+    # a zero potential, so the dense cell stays together through the push
+    zero = np.zeros((sim.p.nny, sim.p.nnx))
+    sim.set_phi(zero)
+    ora.set_phi(zero)
+    st, t, tin_e, tin_i = ora.get_time()
+    sim.set_time(st, t, tin_e, tin_i)
+    sim.charge_deposition()
+    ora.deposit()
+    np.testing.assert_array_equal(sim.rho_fixed(0), ora.rho_fixed(), err_msg="standalone deposit")
+    assert sim.row_counts(0)[5] > n
+    sim.field_solver()
+    ora.field()
+    sim.particle_mover()
+    ora.push(0)
+    sim.cc(t)
+    ora.inject(t)
+    check_state(sim, ora)

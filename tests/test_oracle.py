@@ -66,7 +66,7 @@ def test_single_particle_cic_weights(O, fp64):
     if not fp64:
         acc = o.rho_fixed()
         assert acc.sum() == 2 ** 32  # exactly one unit of charge
-        assert acc[6, 4] == int(0.75 * 65536) * int(0.25 * 65536)
+        assert acc[6, 4] == int(0.75 * 0.25 * 2 ** 32)
 
 
 def test_seam_fold_x0_and_xLx(O):

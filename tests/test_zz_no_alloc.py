@@ -2,8 +2,8 @@
 
 Some callers of this library cannot allocate device memory at the moment they
 need a solve:
-- code running inside a CUDA stream capture;
-- real-time loops that forbid allocation after start-up;
+- real-time loops that forbid allocation after start-up, since an allocation
+  can block for an unbounded time;
 - applications whose device memory all comes from their own pool.
 They pass their own charge, potential and field buffers, and the solver's
 scratch is a static device array inside the library.
