@@ -17,6 +17,11 @@ roofline   the dominant kernel's algorithmic bytes per launch / its mean
 cpu_baseline  the CPU oracle (the reference algorithm restated, FP64,
            OpenMP) on a strip of the same workload, rank 0 only
 --impl reference  the same CPU oracle as the timed arm on the same metric
+batched, serving, precision  (default run, N = 1) the other forms on the same
+           GPU: 256 probe-bias instances stepped together against one at a
+           time; a 32-request Poisson stream at 100/s served by continuous
+           batching against one at a time (solves/s, p50, p99); the
+           precision form of the workload
 
 For N > 1 (torchrun), every rank runs an independent replica on its own GPU
 (no collective on the data path); value sums particle-steps over ranks and
@@ -74,6 +79,10 @@ def parse():
     ap.add_argument("--sweeps", type=int, default=200,
                     help="batched and serving: Jacobi sweeps per step of every instance")
     ap.add_argument("--no-plain", action="store_true", help="batched: skip the one-at-a-time run")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="large: leave out the batched, serving and precision sub-objects")
+    ap.add_argument("--form-steps", type=int, default=10,
+                    help="large: timed steps of the batched and precision sub-objects")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncy", type=int, default=0,
@@ -421,6 +430,17 @@ def run_cupic(args, world, rank, local):
         cb = cpu_strip(p, args.cpu_rows, steps=8, warmup=1, target_s=1.5)
         cpu = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
 
+    plan = dict(zip(("ctas", "rows_per_cta", "halo_depth"), sim.solver_plan()))
+    sim.close()
+    forms = {}
+    if rank == 0 and world == 1 and args.workload == "large" and not args.no_forms \
+            and not args.ncy and not args.ppc:
+        # the second half of the metric: bias-point solves/s and p50/p99
+        # against the plain one-at-a-time method on the same GPU
+        forms["batched"] = bench_batched(256, 200, args.form_steps, args.warmup, local)
+        forms["serving"] = bench_serving(32, 100.0, 300, 200, local)
+        forms["precision"] = bench_precision(args.form_steps, 1, local)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -435,8 +455,7 @@ def run_cupic(args, world, rank, local):
                        "l2": "inputs larger than L2 (particle arrays 3.4 GB); the 4 MB mesh "
                              "stays L2/shared-memory resident by design",
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "jacobi_plan": dict(zip(("ctas", "rows_per_cta", "halo_depth"),
-                                               sim.solver_plan()))},
+                       "jacobi_plan": plan},
             "e2e": e2e,
             "gpu_launches": kernels_per_step(p) * args.steps,
             "roofline": dominant,
@@ -446,41 +465,57 @@ def run_cupic(args, world, rank, local):
             "clocks": clocks,
             "device_flags": flags,
         }
+        line.update(forms)
         print(json.dumps(line), flush=True)
-    sim.close()
     return 0
 
 
-def run_batched(args, local):
+def bench_batched(instances, sweeps, k, warmup, local, plain_run=True):
     """The batched form: probe-bias instances of uneven sizes stepped
-    together, against the same instances stepped one at a time."""
+    together, against the same instances stepped one at a time (each its own
+    graph, one after another).  Both runs start from the same initial
+    states and take the same steps, so every instance's results must be
+    identical; the line says whether they are."""
+    import numpy as np
+
     import cupic_gb300 as cg
     from cupic_gb300.params import bias_instances
-    ps = bias_instances(args.instances, seed=2, sweeps=args.sweeps)
-    sims = []
-    for p in ps:
-        s = cg.Sim(p, device=local)
-        s.init_plasma()
-        sims.append(s)
+    ps = bias_instances(instances, seed=2, sweeps=sweeps)
+
+    def make():
+        out = []
+        for p in ps:
+            s = cg.Sim(p, device=local)
+            s.init_plasma()
+            out.append(s)
+        return out
+
+    sims = make()
     parts = float(sum(sum(s.counts()) for s in sims))
-    k = args.steps
-    # plain: each instance alone, its own graph, one after another
     plain_s = float("nan")
-    if not args.no_plain:
-        for s in sims:
-            s.step(args.warmup)
+    same = None
+    if plain_run:
+        alone = make()
+        for s in alone:
+            s.step(warmup)
         t0 = time.perf_counter()
-        for s in sims:
+        for s in alone:
             s.step(k)
         plain_s = time.perf_counter() - t0
     b = cg.Batch(sims, device=local)
-    b.step(args.warmup)
+    b.step(warmup)
     sampler = ClockSampler(local)
     sampler.start()
     t0 = time.perf_counter()
     b.step(k)
     batch_s = time.perf_counter() - t0
     clocks = sampler.stop()
+    if plain_run:
+        same = all(np.array_equal(a.phi(), m.phi()) and a.stats(k) == m.stats(k)
+                   and all(np.array_equal(a.particles(sp), m.particles(sp)) for sp in (0, 1))
+                   for a, m in zip(alone, sims))
+        for s in alone:
+            s.close()
     n = len(sims)
     line = {
         "metric": "instance-steps/s, probe-bias instances of uneven sizes (batched form)",
@@ -489,32 +524,45 @@ def run_batched(args, local):
         "particle_steps_per_s": parts * k / batch_s,
         "plain": {"value": n * k / plain_s, "particle_steps_per_s": parts * k / plain_s,
                   "ms_per_step_all_instances": 1e3 * plain_s / k},
-        "speedup_vs_plain": plain_s / batch_s, "dtype": "f32", "data": "synthetic",
+        "speedup_vs_plain": plain_s / batch_s, "results_identical_to_plain": same,
+        "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"{n} instances: Nx in {{32,64,128,256}}, Ny=4Nx, 10-50 particles "
                                f"per cell per species, phi_p in [-10,2], mi/me=1836, Ti/Te=0.1, "
-                               f"{args.sweeps} Jacobi sweeps, seeds from 2",
-                   "particles": parts, "cells": sum(p.ncx * p.ncy for p in ps)},
+                               f"{sweeps} Jacobi sweeps, seeds from 2",
+                   "particles": parts, "cells": sum(p.ncx * p.ncy for p in ps),
+                   "timing": "host wall clock around k batched steps (one graph launch per "
+                             "step, synchronised at the end) and around the k steps of every "
+                             "instance stepped alone"},
         "clocks": clocks,
     }
     b.close()
     for s in sims:
         s.close()
+    return line
+
+
+def run_batched(args, local):
+    line = bench_batched(args.instances, args.sweeps, args.steps, args.warmup, local,
+                         plain_run=not args.no_plain)
     print(json.dumps(line), flush=True)
     return 0
 
 
-def run_serving(args, local):
+def bench_serving(requests, rate, solve_steps, sweeps, local):
     """The serving loop against the plain one-at-a-time method on the same
     Poisson request stream; every result must be identical."""
     import copy
     from cupic_gb300 import serve
     from cupic_gb300.params import bias_instances
-    ps = bias_instances(args.requests, seed=3, sweeps=args.sweeps)
-    t = serve.poisson_arrivals(args.requests, args.rate, seed=3)
-    reqs = [serve.Request(k, p, float(t[k]), steps=args.solve_steps,
-                          window=min(1000, args.solve_steps // 2)) for k, p in enumerate(ps)]
+    ps = bias_instances(requests, seed=3, sweeps=sweeps)
+    t = serve.poisson_arrivals(requests, rate, seed=3)
+    reqs = [serve.Request(k, p, float(t[k]), steps=solve_steps,
+                          window=min(1000, solve_steps // 2)) for k, p in enumerate(ps)]
     plain = serve.serve_plain(copy.deepcopy(reqs), device=local)
+    sampler = ClockSampler(local)
+    sampler.start()
     mixed = serve.serve_batched(copy.deepcopy(reqs), device=local)
+    clocks = sampler.stop()
     sp, sm = serve.summary(plain), serve.summary(mixed)
     same = all(a.current == b.current for a, b in
                zip(sorted(plain, key=lambda r: r.rid), sorted(mixed, key=lambda r: r.rid)))
@@ -524,14 +572,48 @@ def run_serving(args, local):
         "p50_ms": sm["p50_ms"], "p99_ms": sm["p99_ms"], "failed": sm["failed"],
         "plain": sp, "speedup_vs_plain": sm["solves_per_s"] / max(sp["solves_per_s"], 1e-30),
         "results_identical_to_plain": same, "dtype": "f32", "data": "synthetic",
-        "config": {"requests": args.requests, "rate_per_s": args.rate,
-                   "steps_per_request": args.solve_steps, "window": reqs[0].window,
-                   "jacobi_sweeps_per_step": args.sweeps,
+        "config": {"requests": requests, "rate_per_s": rate,
+                   "steps_per_request": solve_steps, "window": reqs[0].window,
+                   "jacobi_sweeps_per_step": sweeps,
                    "sizes": "Nx in {32,64,128,256}, Ny=4Nx, 10-50 ppc, phi_p in [-10,2]",
                    "admission": "16 B per particle + 12 B per cell within 96 GiB"},
+        "clocks": clocks,
     }
+    return line
+
+
+def run_serving(args, local):
+    line = bench_serving(args.requests, args.rate, args.solve_steps, args.sweeps, local)
     print(json.dumps(line), flush=True)
     return 0
+
+
+def bench_precision(k, warmup, local):
+    """The precision form of the 512x2048 workload: FP32 sweeps on a
+    correction, an FP64 residual and update every 32 sweeps, to an FP64
+    residual of 1e-10 or 2000 sweeps a step."""
+    import cupic_gb300 as cg
+    p = cg.workload_params("precision")
+    sim = cg.Sim(p, device=local)
+    sim.init_plasma()
+    sim.step(warmup)
+    sampler = ClockSampler(local)
+    sampler.start()
+    total_ms, phases = sim.step_timed(k)
+    clocks = sampler.stop()
+    st = sim.stats(k)
+    parts = float(sum(sum(s["live"]) for s in st)) / k
+    line = {"metric": METRIC, "value": parts * k / (total_ms / 1e3), "unit": UNIT, "steps": k,
+            "warmup": warmup, "ms_per_step": total_ms / k,
+            "solve_ms_per_step": phases["solve"] / k,
+            "sweeps_per_step": statistics.mean(s["sweeps"] for s in st),
+            "last_residual": st[-1]["residual"],
+            "dtype": "f32 sweeps, f64 residual and correction every 32 sweeps",
+            "config": {"workload": workload_desc(p)},
+            "error_vs_fp64": "tests/test_gpu_fp64_contract.py prints it",
+            "clocks": clocks}
+    sim.close()
+    return line
 
 
 def main():

@@ -639,7 +639,7 @@ int sync_check(cupic_ctx *c) {
 int read_ctl_flags(cupic_ctx *c, uint32_t *out) {
   uint32_t f[2];
   CU(cudaMemcpy(f, &c->ctl->flags, sizeof(f), cudaMemcpyDeviceToHost));
-  *out = f[0] | f[1];
+  *out = f[0] | f[1] | c->host_flags;
   return CUPIC_OK;
 }
 
@@ -668,26 +668,37 @@ int finish(cupic_ctx *c) {
 // One step: solve + field, then the injection draws on the side stream while
 // the main stream clears the next charge, pushes and appends the movers;
 // the injected particles are appended once both branches are done.
-int enqueue_after_solve(cupic_ctx *c, bool zeroed) {
+// marks: null, or CUPIC_NPHASE events recorded on the main stream after the
+// solve, the clearing, the push, the arrivals (with the wait for the draws
+// and the room check), the append and the bookkeeping -- the phases of
+// cupic_step_timed.
+int enqueue_after_solve(cupic_ctx *c, bool zeroed, const cudaEvent_t *marks = nullptr) {
+  auto mark = [&](int k) { return marks ? cudaEventRecord(marks[k], c->stream) : cudaSuccess; };
+  CU(mark(0));
   CU(cudaEventRecord(c->ev_fork, c->stream));
   CU(cudaStreamWaitEvent(c->side, c->ev_fork, 0));
   CU(launch_inject_draw(c->a, c->side));
   CU(cudaEventRecord(c->ev_join, c->side));
   if (!zeroed) CU(launch_zero_next_rho(c->a, c->stream));
+  CU(mark(1));
   CU(launch_push_deposit(c->a, c->stream));
+  CU(mark(2));
   CU(cudaStreamWaitEvent(c->stream, c->ev_join, 0));
   CU(launch_room(c->a, c->stream));
   CU(launch_arrive(c->a, c->stream));
+  CU(mark(3));
   CU(launch_inject_append(c->a, c->stream));
+  CU(mark(4));
   CU(launch_finalize(c->a, c->stream));
+  CU(mark(5));
   return CUPIC_OK;
 }
 
-int enqueue_step(cupic_ctx *c) {
+int enqueue_step(cupic_ctx *c, const cudaEvent_t *marks = nullptr) {
   bool zeroed = false;
   int rc = run_step_solve(c, &zeroed);
   if (rc) return rc;
-  return enqueue_after_solve(c, zeroed);
+  return enqueue_after_solve(c, zeroed, marks);
 }
 
 int capture_step(cupic_ctx *c) {
@@ -864,8 +875,12 @@ int complete_halted(cupic_ctx *c, int32_t skipped) {
 }
 
 // Waits for the context's work; a run that the room check halted is
-// completed first, as often as it halts again.
+// completed first, as often as it halts again.  When its rows cannot grow,
+// the run stays halted: the context keeps CUPIC_FLAG_CAPACITY and every
+// later call that needs its state returns the growth's status, until
+// cupic_clear_flags.
 int settle(cupic_ctx *c) {
+  if (c->grow_status) return c->grow_status;
   for (;;) {
     CU(cudaStreamSynchronize(c->stream));
     int32_t hs[2];
@@ -873,7 +888,11 @@ int settle(cupic_ctx *c) {
     CU(cudaMemcpy(hs, &c->ctl->halt, sizeof(hs), cudaMemcpyDeviceToHost));
     if (!hs[0]) return CUPIC_OK;
     const int rc = complete_halted(c, hs[1]);
-    if (rc) return rc;
+    if (rc) {
+      c->host_flags |= CUPIC_FLAG_CAPACITY;
+      c->grow_status = rc;
+      return rc;
+    }
   }
 }
 
@@ -1516,60 +1535,42 @@ int cupic_step_timed(cupic_ctx *c, int32_t nsteps, float *phase_ms, int32_t npha
     int rc = deposit_current(c);
     if (rc) return rc;
   }
+  // the step's own launch sequence (enqueue_step, the one its graph
+  // captures), launched directly with an event after each phase
   const int per = CUPIC_NPHASE;
-  std::vector<cudaEvent_t> ev((size_t)nsteps * per + 1, nullptr);
+  std::vector<cudaEvent_t> ev((size_t)nsteps * per + 2, nullptr);
   int rc = CUPIC_OK;
   for (auto &e : ev)
     if (cudaEventCreate(&e) != cudaSuccess) rc = CUPIC_ERR_CUDA;
-  const cupic_params &p = c->p;
-  JacobiArgs J = jargs(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1);
-  J.zero_next = 1;  // as in a step: the solve clears the next charge accumulator
   cudaError_t e = rc ? cudaErrorUnknown : cudaEventRecord(ev[0], c->stream);
-  for (int s = 0; s < nsteps && e == cudaSuccess; ++s) {
-    // the launch order of enqueue_step, with an event after each
-    // main-stream kernel; the arrive phase is the wait for the side branch
-    // (draws), the room check and the arrivals
-    cudaEvent_t *q = &ev[(size_t)s * per + 1];
-    if (c->p.refine_every > 0) {
-      const int r = run_solve(c, p.tol, p.min_sweeps, p.max_sweeps, p.check_every, 1);
-      if (r) rc = r;
-      e = r ? cudaErrorUnknown : cudaSuccess;
-    } else {
-      e = launch_jacobi(c->a, J, c->stream);
-    }
-    if (e == cudaSuccess) e = cudaEventRecord(q[0], c->stream);
-    if (e == cudaSuccess) e = cudaEventRecord(c->ev_fork, c->stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->side, c->ev_fork, 0);
-    if (e == cudaSuccess) e = launch_inject_draw(c->a, c->side);
-    if (e == cudaSuccess) e = cudaEventRecord(c->ev_join, c->side);
-    if (e == cudaSuccess && c->p.refine_every > 0) e = launch_zero_next_rho(c->a, c->stream);
-    if (e == cudaSuccess) e = cudaEventRecord(q[1], c->stream);
-    if (e == cudaSuccess) e = launch_push_deposit(c->a, c->stream);
-    if (e == cudaSuccess) e = cudaEventRecord(q[2], c->stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(c->stream, c->ev_join, 0);
-    if (e == cudaSuccess) e = launch_room(c->a, c->stream);
-    if (e == cudaSuccess) e = launch_arrive(c->a, c->stream);
-    if (e == cudaSuccess) e = cudaEventRecord(q[3], c->stream);
-    if (e == cudaSuccess) e = launch_inject_append(c->a, c->stream);
-    if (e == cudaSuccess) e = cudaEventRecord(q[4], c->stream);
-    if (e == cudaSuccess) e = launch_finalize(c->a, c->stream);
-    if (e == cudaSuccess) e = cudaEventRecord(q[5], c->stream);
-    if (e == cudaSuccess) c->host_cur ^= 1;
+  for (int s = 0; s < nsteps && e == cudaSuccess && !rc; ++s) {
+    rc = enqueue_step(c, &ev[(size_t)s * per + 1]);
+    if (!rc) c->host_cur ^= 1;
   }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e == cudaSuccess && !rc) e = cudaStreamSynchronize(c->stream);
+  // a run halted by the room check is completed (rows grown, the halted
+  // step finished, the skipped steps run) inside the timed region
+  int32_t halted = 0;
+  if (e == cudaSuccess && !rc) e = cudaMemcpy(&halted, &c->ctl->halt, sizeof(halted), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess && !rc && halted) {
+    rc = settle(c);
+    if (!rc) e = cudaEventRecord(ev.back(), c->stream);
+    if (e == cudaSuccess && !rc) e = cudaStreamSynchronize(c->stream);
+  }
   for (int k = 0; k < nphase; ++k) phase_ms[k] = 0.0f;
-  if (e == cudaSuccess) {
+  if (e == cudaSuccess && !rc) {
     for (int s = 0; s < nsteps && e == cudaSuccess; ++s)
       for (int k = 0; k < per && e == cudaSuccess; ++k) {
         float ms = 0.0f;
         e = cudaEventElapsedTime(&ms, ev[(size_t)s * per + k], ev[(size_t)s * per + k + 1]);
         phase_ms[k] += ms;
       }
-    if (e == cudaSuccess) e = cudaEventElapsedTime(total_ms, ev[0], ev.back());
+    if (e == cudaSuccess) e = cudaEventElapsedTime(total_ms, ev[0], halted ? ev.back() : ev[ev.size() - 2]);
   }
   for (auto &x : ev)
     if (x) cudaEventDestroy(x);
-  if (e != cudaSuccess) return rc ? rc : cuda_status(e);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_status(e);
   return finish(c);
 }
 
@@ -1722,7 +1723,8 @@ int cupic_density_profile(cupic_ctx *c, int species, double *density) {
 int cupic_get_flags(cupic_ctx *c, uint32_t *flags) {
   if (!c || !flags) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
-  SETTLE(c);
+  const int rc = settle(c);
+  if (rc && !c->grow_status) return rc;  // a failed growth is reported as a flag
   return read_ctl_flags(c, flags);
 }
 
@@ -1736,6 +1738,9 @@ int cupic_test_bounded_wait(cupic_ctx *c) {
 int cupic_clear_flags(cupic_ctx *c) {
   if (!c) return CUPIC_ERR_ARG;
   CU(cudaSetDevice(c->device));
+  // a run whose rows could not grow is retried by the next call
+  c->host_flags = 0;
+  c->grow_status = 0;
   SETTLE(c);
   uint32_t z[2] = {0u, 0u};
   int32_t zero = 0;

@@ -49,6 +49,11 @@ struct cupic_ctx {
   // advanced whenever rows or staging rows move to new buffers (a batch
   // holding this context's SimArgs rebuilds)
   int layout_epoch = 0;
+  // CUPIC_FLAG_* raised on the host: a halted run whose rows could not grow
+  // (no memory, or a row past 2^31 places) stays halted and reports
+  // CUPIC_FLAG_CAPACITY with the device's flags until the flags are cleared
+  uint32_t host_flags = 0;
+  int grow_status = 0;  // the status that growth failed with
 };
 
 // status helpers of capi.cu used by batch.cu

@@ -225,9 +225,12 @@ enum {
   CUPIC_PHASE_FINAL = 5,  /* per-step counters and clock */
   CUPIC_NPHASE = 6
 };
-/* nsteps cycles launched one kernel at a time with a CUDA event between
- * kernels on the context's stream; phase_ms[k] = device ms of phase k summed
- * over the steps, *total_ms = device ms from the first to the last event. */
+/* nsteps cycles of the step's own launch sequence (the one cupic_step's
+ * graph captures), launched directly with a CUDA event after each phase on
+ * the context's stream; phase_ms[k] = device ms of phase k summed over the
+ * steps, *total_ms = device ms from the first to the last event.  A run that
+ * the room check halts is completed inside the timed region (*total_ms then
+ * runs to the end of the completion). */
 int cupic_step_timed(struct cupic_ctx *ctx, int32_t nsteps, float *phase_ms, int32_t nphase,
                      float *total_ms);
 

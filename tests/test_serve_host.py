@@ -60,3 +60,74 @@ def test_summary_counts_failed_requests_apart():
 def test_summary_of_a_stream_where_every_request_failed():
     s = serve.summary([request(0, 0.0, 0.0, 1.0, error="device flags 0x4")])
     assert s["solves"] == 0 and s["failed"] == 1 and s["solves_per_s"] == 0.0
+
+
+class FakeSim:
+    """Stands in for a context: `fail_at` steps in, its rows cannot grow,
+    which the library reports as CUPIC_FLAG_CAPACITY (0x2) on the context."""
+
+    def __init__(self, params, device=0):
+        self.p = params
+        self.done = 0
+        self.fail_at = getattr(params, "fail_at", None)
+
+    def init_plasma(self, wait=True):
+        pass
+
+    def sync(self):
+        pass
+
+    def failed(self):
+        return self.fail_at is not None and self.done >= self.fail_at
+
+    def flags(self):
+        return 0x2 if self.failed() else 0
+
+    def probe_current(self, window):
+        return float(self.p.rid)
+
+    def close(self):
+        pass
+
+
+class FakeBatch:
+    def __init__(self, sims=(), device=0):
+        self.members = list(sims)
+
+    def set(self, sims):
+        self.members = list(sims)
+
+    def step(self, n=1, sync=True):
+        for s in self.members:
+            s.done += n
+
+    def sync(self):
+        if any(s.failed() for s in self.members):
+            from cupic_gb300 import CupicError
+            raise CupicError(5, "batch_sync")
+
+    def close(self):
+        pass
+
+
+class FakeParams:
+    def __init__(self, rid, fail_at=None):
+        self.rid, self.fail_at = rid, fail_at
+        self.ncx, self.ncy, self.ppr = 32, 128, 320
+        self.check_every = self.max_sweeps = self.init_max_sweeps = 200
+
+
+def test_a_request_whose_rows_cannot_grow_fails_alone(monkeypatch):
+    """A member whose halted run cannot grow its rows reports the capacity
+    flag; the serving loop ends that request with its error and finishes
+    the others with their own results."""
+    monkeypatch.setattr(serve, "Sim", FakeSim)
+    monkeypatch.setattr(serve, "Batch", FakeBatch)
+    monkeypatch.setattr(serve, "reserve", lambda *a, **k: None)
+    reqs = [serve.Request(k, FakeParams(k, fail_at=30 if k == 1 else None), 0.0, steps=100,
+                          window=50) for k in range(3)]
+    out = serve.serve_batched(reqs, tick=20)
+    byid = {r.rid: r for r in out}
+    assert byid[1].error == "device flags 0x2" and byid[1].current is None
+    assert byid[0].current == 0.0 and byid[2].current == 2.0
+    assert byid[0].error is None and byid[2].error is None
