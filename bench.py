@@ -520,7 +520,7 @@ def bench_batched(instances, sweeps, k, warmup, local, plain_run=True):
     line = {
         "metric": "instance-steps/s, probe-bias instances of uneven sizes (batched form)",
         "value": n * k / batch_s, "unit": "instance-steps/s", "n_gpus": 1, "steps": k,
-        "warmup": args.warmup, "ms_per_step": 1e3 * batch_s / k, "higher_is_better": True,
+        "warmup": warmup, "ms_per_step": 1e3 * batch_s / k, "higher_is_better": True,
         "particle_steps_per_s": parts * k / batch_s,
         "plain": {"value": n * k / plain_s, "particle_steps_per_s": parts * k / plain_s,
                   "ms_per_step_all_instances": 1e3 * plain_s / k},
