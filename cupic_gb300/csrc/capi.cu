@@ -1247,6 +1247,20 @@ int cupic_reserve(int device, uint64_t bytes, int32_t contexts) {
     keep_stream_set(device, s);
   }
   if (bytes == 0) return CUPIC_OK;
+  // Grow the pool only when the memory it already holds and does not use
+  // falls short.  A pool that earlier contexts have left holding freed
+  // memory in many pieces must not be grown past it: after such a growth
+  // every context created while the device is busy waited for the device
+  // (52 ms each in a serving run after 512 contexts had come and gone,
+  // against 0.05 ms without the growth).
+  {
+    cudaMemPool_t pool;
+    CU(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t reserved = 0, used = 0;
+    CU(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved));
+    CU(cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used));
+    if (reserved >= used && reserved - used >= bytes) return CUPIC_OK;
+  }
   cudaStream_t st = nullptr;
   CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
   void *p = nullptr;

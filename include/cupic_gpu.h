@@ -157,11 +157,12 @@ int cupic_init_plasma_nowait(struct cupic_ctx *ctx);
 /* Contexts take their device memory from the device's stream-ordered pool
  * (cudaMallocAsync), which keeps freed memory for later contexts, and their
  * streams from a per-device set that destroyed contexts return theirs to.
- * This grows the pool to at least `bytes` and the set to `contexts` streams'
- * worth now, so that contexts created later (a server admitting requests
- * while the device steps others) neither map new pages nor create streams,
- * which can stall while the device is busy.  Both are kept until the
- * process exits. */
+ * This grows the pool to at least `bytes` of free memory (it allocates
+ * nothing when the pool already holds that much unused) and the set to
+ * `contexts` streams' worth now, so that contexts created later (a server
+ * admitting requests while the device steps others) neither map new pages
+ * nor create streams, which can stall while the device is busy.  Both are
+ * kept until the process exits. */
 int cupic_reserve(int device, uint64_t bytes, int32_t contexts);
 
 /* Replaces one species with n particles given as the reference's particle
