@@ -502,7 +502,10 @@ def bench_batched(instances, sweeps, k, warmup, local, plain_run=True):
         for s in alone:
             s.step(k)
         plain_s = time.perf_counter() - t0
-    b = cg.Batch(sims, device=local)
+    t0 = time.perf_counter()
+    b = cg.Batch(sims, device=local)  # builds the arrays, tunes the solve layout
+    build_s = time.perf_counter() - t0
+    layout = dict(zip(("depth_cap", "cta_mult", "ctas"), b.plan()))
     b.step(warmup)
     sampler = ClockSampler(local)
     sampler.start()
@@ -530,6 +533,7 @@ def bench_batched(instances, sweeps, k, warmup, local, plain_run=True):
                                f"per cell per species, phi_p in [-10,2], mi/me=1836, Ti/Te=0.1, "
                                f"{sweeps} Jacobi sweeps, seeds from 2",
                    "particles": parts, "cells": sum(p.ncx * p.ncy for p in ps),
+                   "solve_layout": layout, "build_and_tune_s": build_s,
                    "timing": "host wall clock around k batched steps (one graph launch per "
                              "step, synchronised at the end) and around the k steps of every "
                              "instance stepped alone"},

@@ -42,7 +42,7 @@ EXPORTED = [
     "cupic_write_bins_file", "cupic_rewrite_input_data", "cupic_particles_snapshot",
     "cupic_mesh_snapshot", "cupic_save_bm", "cupic_save_bins", "cupic_load_particles_file",
     "cupic_batch_create", "cupic_batch_set", "cupic_batch_step", "cupic_batch_sync",
-    "cupic_batch_destroy", "cupic_probe_current", "cupic_density_profile",
+    "cupic_batch_plan", "cupic_batch_destroy", "cupic_probe_current", "cupic_density_profile",
     "cupic_test_bounded_wait", "cupic_init_plasma_nowait", "cupic_reserve",
 ]
 
@@ -132,6 +132,7 @@ def load_library(build_if_missing=False):
         "cupic_batch_set": [vp, P(vp), c_i32],
         "cupic_batch_step": [vp, c_i32],
         "cupic_batch_sync": [vp],
+        "cupic_batch_plan": [vp, P(c_i32), P(c_i32), P(c_i32)],
         "cupic_batch_destroy": [vp],
         "cupic_probe_current": [vp, c_i32, P(c_d)],
         "cupic_density_profile": [vp, c_i, P(c_d)],
@@ -465,6 +466,13 @@ class Batch:
 
     def sync(self):
         _ok(self.L.cupic_batch_sync(self.h), "batch_sync")
+
+    def plan(self):
+        """The batched solve's layout: (halo depth cap, CTA multiple, CTAs)."""
+        d, m, n = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _ok(self.L.cupic_batch_plan(self.h, ctypes.byref(d), ctypes.byref(m), ctypes.byref(n)),
+            "batch_plan")
+        return d.value, m.value, n.value
 
     def close(self):
         if getattr(self, "h", None) and self.h.value:

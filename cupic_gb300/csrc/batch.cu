@@ -22,11 +22,15 @@
 // alone (its kernels return at once); the batch's sync grows its rows and
 // completes its steps with the single-context step, and the next batched
 // step rebuilds the arrays.
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 #include <new>
 #include <numeric>
+#include <tuple>
 #include <vector>
 
 #include "ctx.h"
@@ -63,6 +67,8 @@ struct cupic_batch {
   size_t nflags = 0, jsmem = 0;
   cudaGraphExec_t graph = nullptr;
   bool graph_ok = false;
+  // the batched solve's layout knobs in use: halo depth cap, CTA multiple
+  int knob_depth = 4, knob_mult = 1;
 };
 
 namespace {
@@ -96,45 +102,58 @@ void drop_graph(cupic_batch *b) {
   b->graph_ok = false;
 }
 
-// the batched solve's layout of one instance: the fewest CTAs whose shared
-// memory holds its rows, with a halo depth of up to kBatchDepth (over the
-// 256-instance mix, depths of 2, 3, 4, 6, 8 and 16 gave 15.1, 14.6, 14.4,
-// 14.8, 14.6 and 16.1 ms per batched step)
-constexpr int kBatchDepth = 4;
+// The batched solve's layout of one instance: the fewest CTAs whose shared
+// memory holds its rows (tile height B = ceil(rows / G)), times a CTA
+// multiple, with a halo depth of up to a cap.  The depth cap and the
+// multiple are the two knobs of the batched-solve autotuner (tune_solve);
+// without tuning they are 4 and 1 (over the 256-instance mix, depths of 2,
+// 3, 4, 6, 8 and 16 gave 15.1, 14.6, 14.4, 14.8, 14.6 and 16.1 ms per
+// batched step).
+struct Knobs {
+  int depth, mult;
+  bool operator<(const Knobs &o) const { return depth != o.depth ? depth < o.depth : mult < o.mult; }
+};
+constexpr Knobs kDefaultKnobs{4, 1};
+constexpr Knobs kCandidates[] = {{1, 1}, {2, 1}, {4, 1}, {8, 1}, {2, 2}, {4, 2}, {8, 2}};
+constexpr int kTuneMembers = 16;  // batches this large tune their solve layout
 struct Plan {
   int G, B, K, P;
   size_t smem;
 };
 
 // the layout on G > 1 CTAs, if their shared memory holds it
-bool plan_on(const SimArgs &a, int G, long long rows_fit, Plan *out) {
+bool plan_on(const SimArgs &a, int G, long long rows_fit, int kcap, Plan *out) {
   const int M = a.nny - 2;
   const int P = (a.nnx + 3) / 4 * 4;
   const int B = (M + G - 1) / G;
-  const int K = std::min(kBatchDepth, M / G);
+  const int K = std::min(kcap, M / G);
   if (G < 2 || K < 1 || B + 2 * K > rows_fit) return false;
   *out = {G, B, K, P, jacobi_smem_bytes(B, K, P)};
   return true;
 }
 
-bool plan_instance(const SimArgs &a, long long rows_fit, Plan *out) {
+bool plan_instance(const SimArgs &a, long long rows_fit, const Knobs &k, Plan *out) {
   const int M = a.nny - 2;
   const int P = (a.nnx + 3) / 4 * 4;
+  Plan base{};
+  bool ok = false;
   if (M + 2 <= rows_fit) {
-    *out = {1, M, 1, P, jacobi_smem_bytes(M, 1, P)};
-    return true;
+    base = {1, M, 1, P, jacobi_smem_bytes(M, 1, P)};
+    ok = true;
   }
-  for (int G = 2; G <= M; ++G)
-    if (plan_on(a, G, rows_fit, out)) return true;
-  return false;
+  for (int G = 2; !ok && G <= M; ++G) ok = plan_on(a, G, rows_fit, k.depth, &base);
+  if (!ok) return false;
+  Plan q;
+  if (k.mult > 1 && plan_on(a, std::min(M, base.G * k.mult), rows_fit, k.depth, &q)) base = q;
+  *out = base;
+  return true;
 }
 
-int build(cupic_batch *b) {
-  drop_graph(b);
+// The solve's part of the batch arrays for the given knobs: every member's
+// plan, the CTA groups and their instance lists, the exchange buffers and
+// the JacobiArgs.  The stream is idle.
+int layout_solve(cupic_batch *b, const Knobs &kn) {
   const int n = (int)b->members.size();
-  b->epochs.clear();
-  for (const cupic_ctx *c : b->members) b->epochs.push_back(c->layout_epoch);
-  if (n == 0) return CUPIC_OK;
   int dev_max = 0;
   CU(cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device));
   std::vector<SimArgs> inst(n);
@@ -142,19 +161,15 @@ int build(cupic_batch *b) {
   std::vector<double> work(n);
   std::vector<long long> fit(n);
   size_t smem = 0;
-  b->max_nnx = b->max_ncy = b->max_inj = 0;
   for (int i = 0; i < n; ++i) {
     const cupic_ctx *c = b->members[i];
     inst[i] = c->a;
     const long long P = (c->a.nnx + 3) / 4 * 4;
     const long long rows_fit = (long long)((dev_max - 1024) / (3 * sizeof(float) * P));
     fit[i] = rows_fit;
-    if (!plan_instance(c->a, rows_fit, &plan[i])) return CUPIC_ERR_ARG;
+    if (!plan_instance(c->a, rows_fit, kn, &plan[i])) return CUPIC_ERR_ARG;
     smem = std::max(smem, plan[i].smem);
     work[i] = (double)c->a.nnx * c->a.nny * std::max(c->p.max_sweeps, 1);
-    b->max_nnx = std::max(b->max_nnx, c->a.nnx);
-    b->max_ncy = std::max(b->max_ncy, c->a.ncy);
-    b->max_inj = std::max({b->max_inj, c->a.sp[0].inj_cap, c->a.sp[1].inj_cap});
   }
   CU(jacobi_batch_set_smem(smem));
   int per_sm = 0;
@@ -169,7 +184,7 @@ int build(cupic_batch *b) {
     const int share = (int)(T * work[i] / wsum);
     const int want = std::min(b->members[i]->jG, share);
     Plan q;
-    if (want > plan[i].G && plan_on(inst[i], want, fit[i], &q) && q.smem <= smem) plan[i] = q;
+    if (want > plan[i].G && plan_on(inst[i], want, fit[i], kn.depth, &q) && q.smem <= smem) plan[i] = q;
   }
   // buckets of equal CTA count; groups per bucket by work share
   std::vector<int> sizes;
@@ -285,6 +300,150 @@ int build(cupic_batch *b) {
     oh += (size_t)4 * q.G * q.K * q.P;
     jargs[i] = J;
   }
+  if ((rc = grow(&b->d_groups, &b->cap_groups, groups.size()))) return rc;
+  // d_jargs and d_list hold one entry per member
+  cudaFree(b->d_jargs);
+  cudaFree(b->d_list);
+  b->d_jargs = nullptr;
+  b->d_list = nullptr;
+  CU(cudaMalloc(&b->d_jargs, n * sizeof(JacobiArgs)));
+  CU(cudaMalloc(&b->d_list, n * sizeof(int)));
+  CU(cudaMemcpy(b->d_jargs, jargs.data(), n * sizeof(JacobiArgs), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(b->d_groups, groups.data(), groups.size() * sizeof(JGroup), cudaMemcpyHostToDevice));
+  CU(cudaMemcpy(b->d_list, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice));
+  b->knob_depth = kn.depth;
+  b->knob_mult = kn.mult;
+  return CUPIC_OK;
+}
+
+// device ms of one batched solve with the current layout: the best of two
+// launches after a warm-up one
+int time_solve(cupic_batch *b, float *ms) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  CU(cudaEventCreate(&e0));
+  CU(cudaEventCreate(&e1));
+  float best = 1e30f;
+  cudaError_t e = cudaSuccess;
+  for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+    e = cudaMemsetAsync(b->d_flags, 0, b->nflags * sizeof(unsigned), b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(e0, b->stream);
+    if (e == cudaSuccess)
+      e = launch_jacobi_batch(b->d_inst, b->d_jargs, b->d_groups, b->ngroups, b->d_list, b->nctas,
+                              b->jsmem, b->stream);
+    if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    float t = 0.0f;
+    if (e == cudaSuccess && rep > 0 && cudaEventElapsedTime(&t, e0, e1) == cudaSuccess)
+      best = std::min(best, t);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *ms = 1e30f;
+    return CUPIC_OK;  // the layout is left out
+  }
+  *ms = best;
+  return CUPIC_OK;
+}
+
+// The batched-solve autotuner: times every candidate layout (halo depth cap
+// x CTA multiple, kCandidates) with the members' own meshes and sweep
+// counts, and keeps the fastest.  The trial solves overwrite the members'
+// potential and field and their solver status words; those are saved
+// before and put back after, so the members' results do not depend on the
+// tuning.  The epoch base of the halo words keeps advancing, as the
+// exchange protocol needs.  Picks are cached per process by the members'
+// multiset of (mesh shape, sweeps), and batches of fewer than kTuneMembers
+// members take the default knobs.  CUPIC_BATCH_TUNE=0 turns tuning off.
+struct MixKey {
+  std::vector<std::tuple<int, int, int, int>> shapes;
+  bool operator<(const MixKey &o) const { return shapes < o.shapes; }
+};
+std::mutex g_mix_mu;
+std::map<std::pair<int, MixKey>, Knobs> g_mix_tuned;
+
+int tune_solve(cupic_batch *b) {
+  const int n = (int)b->members.size();
+  const char *env = getenv("CUPIC_BATCH_TUNE");
+  if (n < kTuneMembers || (env && atoi(env) == 0)) return layout_solve(b, kDefaultKnobs);
+  MixKey key;
+  for (const cupic_ctx *c : b->members)
+    key.shapes.emplace_back(c->a.nnx, c->a.nny, c->p.max_sweeps, c->p.check_every);
+  std::sort(key.shapes.begin(), key.shapes.end());
+  {
+    std::lock_guard<std::mutex> lk(g_mix_mu);
+    auto it = g_mix_tuned.find({b->device, key});
+    if (it != g_mix_tuned.end()) return layout_solve(b, it->second);
+  }
+  // save what the trials overwrite
+  size_t nodes = 0;
+  for (const cupic_ctx *c : b->members) nodes += (size_t)c->a.nnx * c->a.nny;
+  constexpr size_t kStat = offsetof(Ctl, residual) + sizeof(float) - offsetof(Ctl, step_flags);
+  unsigned char *save = nullptr;
+  const size_t bytes = nodes * (sizeof(float) + sizeof(float2)) + (size_t)n * (kStat + sizeof(int32_t));
+  CU(cudaMalloc(&save, bytes));
+  auto copy_all = [&](bool back) -> cudaError_t {
+    unsigned char *q = save;
+    cudaError_t e = cudaSuccess;
+    for (const cupic_ctx *c : b->members) {
+      const size_t nn = (size_t)c->a.nnx * c->a.nny;
+      unsigned char *ctlb = reinterpret_cast<unsigned char *>(c->ctl);
+      struct { void *dev; size_t len; } part[] = {
+          {c->a.phi, nn * sizeof(float)}, {c->a.E, nn * sizeof(float2)},
+          {ctlb + offsetof(Ctl, step_flags), kStat}, {ctlb + offsetof(Ctl, abort), sizeof(int32_t)}};
+      for (auto &pt : part) {
+        if (e == cudaSuccess)
+          e = back ? cudaMemcpyAsync(pt.dev, q, pt.len, cudaMemcpyDeviceToDevice, b->stream)
+                   : cudaMemcpyAsync(q, pt.dev, pt.len, cudaMemcpyDeviceToDevice, b->stream);
+        q += pt.len;
+      }
+    }
+    return e;
+  };
+  cudaError_t e = copy_all(false);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  Knobs pick = kDefaultKnobs;
+  float best = 1e30f;
+  int rc = e == cudaSuccess ? CUPIC_OK : CUPIC_ERR_CUDA;
+  for (const Knobs &k : kCandidates) {
+    if (rc) break;
+    if (layout_solve(b, k) != CUPIC_OK) continue;  // this layout does not fit
+    float ms = 1e30f;
+    rc = time_solve(b, &ms);
+    if (!rc && ms < best) {
+      best = ms;
+      pick = k;
+    }
+  }
+  e = copy_all(true);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  cudaFree(save);
+  if (rc) return rc;
+  if (e != cudaSuccess) return CUPIC_ERR_CUDA;
+  {
+    std::lock_guard<std::mutex> lk(g_mix_mu);
+    g_mix_tuned[{b->device, key}] = pick;
+  }
+  return layout_solve(b, pick);
+}
+
+int build(cupic_batch *b) {
+  drop_graph(b);
+  const int n = (int)b->members.size();
+  b->epochs.clear();
+  for (const cupic_ctx *c : b->members) b->epochs.push_back(c->layout_epoch);
+  if (n == 0) return CUPIC_OK;
+  std::vector<SimArgs> inst(n);
+  b->max_nnx = b->max_ncy = b->max_inj = 0;
+  for (int i = 0; i < n; ++i) {
+    const cupic_ctx *c = b->members[i];
+    inst[i] = c->a;
+    b->max_nnx = std::max(b->max_nnx, c->a.nnx);
+    b->max_ncy = std::max(b->max_ncy, c->a.ncy);
+    b->max_inj = std::max({b->max_inj, c->a.sp[0].inj_cap, c->a.sp[1].inj_cap});
+  }
+  int rc;
   // work lists
   std::vector<int2> rows;
   b->max_nnx_short = b->max_nnx_mid = 0;
@@ -304,24 +463,11 @@ int build(cupic_batch *b) {
     if (cls(r.x) == 1) ++b->nrows_mid;
   }
   b->nrows = (int)rows.size();
-  if ((rc = grow(&b->d_inst, &b->cap_inst, (size_t)n)) ||
-      (rc = grow(&b->d_groups, &b->cap_groups, groups.size())) ||
-      (rc = grow(&b->d_rows, &b->cap_rows, rows.size())))
+  if ((rc = grow(&b->d_inst, &b->cap_inst, (size_t)n)) || (rc = grow(&b->d_rows, &b->cap_rows, rows.size())))
     return rc;
-  // d_jargs and d_list share the instance capacity
-  static_assert(sizeof(JacobiArgs) >= sizeof(int), "");
-  cudaFree(b->d_jargs);
-  cudaFree(b->d_list);
-  b->d_jargs = nullptr;
-  b->d_list = nullptr;
-  CU(cudaMalloc(&b->d_jargs, n * sizeof(JacobiArgs)));
-  CU(cudaMalloc(&b->d_list, n * sizeof(int)));
   CU(cudaMemcpy(b->d_inst, inst.data(), n * sizeof(SimArgs), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(b->d_jargs, jargs.data(), n * sizeof(JacobiArgs), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(b->d_groups, groups.data(), groups.size() * sizeof(JGroup), cudaMemcpyHostToDevice));
-  CU(cudaMemcpy(b->d_list, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice));
   CU(cudaMemcpy(b->d_rows, rows.data(), rows.size() * sizeof(int2), cudaMemcpyHostToDevice));
-  return CUPIC_OK;
+  return tune_solve(b);
 }
 
 int enqueue(cupic_batch *b) {
@@ -459,6 +605,14 @@ int cupic_batch_step(cupic_batch *b, int32_t nsteps) {
     }
   }
   for (cupic_ctx *c : b->members) c->host_cur ^= (nsteps & 1);
+  return CUPIC_OK;
+}
+
+int cupic_batch_plan(cupic_batch *b, int32_t *depth_cap, int32_t *cta_mult, int32_t *ctas) {
+  if (!b || !depth_cap || !cta_mult || !ctas) return CUPIC_ERR_ARG;
+  *depth_cap = b->knob_depth;
+  *cta_mult = b->knob_mult;
+  *ctas = b->nctas;
   return CUPIC_OK;
 }
 

@@ -324,6 +324,16 @@ int cupic_batch_set(cupic_batch *b, struct cupic_ctx *const *members, int32_t n)
 int cupic_batch_step(cupic_batch *b, int32_t nsteps);
 /* Waits for the batch; returns the first member's error status, if any. */
 int cupic_batch_sync(cupic_batch *b);
+/* The batched solve's layout: each member's solve takes the fewest CTAs
+ * whose shared memory holds its rows, times *cta_mult, with a halo depth of
+ * at most *depth_cap; *ctas is the launch's CTA count.  When a member set
+ * of 16 or more is built, an autotuner times every candidate (depth cap 1,
+ * 2, 4, 8 x CTA multiple 1, 2) on the members' own meshes -- saving and
+ * restoring their potential, field and solver status -- and keeps the
+ * fastest; picks are cached per process by the members' mesh shapes and
+ * sweep counts.  Smaller sets, or CUPIC_BATCH_TUNE=0, take depth cap 4 and
+ * multiple 1. */
+int cupic_batch_plan(cupic_batch *b, int32_t *depth_cap, int32_t *cta_mult, int32_t *ctas);
 int cupic_batch_destroy(cupic_batch *b);
 
 /* ---- the reference's text files ---------------------------------------- */

@@ -170,3 +170,47 @@ def test_batched_large_member_matches_oracle(gpu_lib):
         ora.close()
         for s in members:
             s.close()
+
+
+def test_tuned_batch_equals_members_alone(gpu_lib, monkeypatch):
+    """A set of 18 members is large enough for the batched-solve autotuner:
+    it times its candidate layouts on the members' own meshes, restores
+    their potential, field and solver status, and the members still get
+    their solo results bit for bit.  A second batch of the same mix takes
+    the cached pick; CUPIC_BATCH_TUNE=0 takes the default layout."""
+    from cupic_gb300.params import bias_instances
+    monkeypatch.delenv("CUPIC_BATCH_TUNE", raising=False)
+    ps = bias_instances(18, seed=5, sizes=(32, 64))
+
+    def make():
+        out = []
+        for p in ps:
+            s = cg.Sim(p)
+            s.init_plasma()
+            out.append(s)
+        return out
+
+    alone, batched = make(), make()
+    try:
+        phi0 = [s.phi() for s in batched]
+        with cg.Batch(batched) as b:
+            depth, mult, ctas = b.plan()
+            assert depth in (1, 2, 4, 8) and mult in (1, 2) and ctas > 0
+            # the trials left every member's potential as it was
+            for k, s in enumerate(batched):
+                np.testing.assert_array_equal(s.phi(), phi0[k], err_msg=f"member {k} phi after tuning")
+                assert s.flags() == 0
+            b.step(4)
+        for s in alone:
+            s.step(4)
+        for k, (a, m) in enumerate(zip(alone, batched)):
+            compare(a, m, f"member {k}")
+            assert a.stats(4) == m.stats(4), f"member {k} stats"
+        with cg.Batch(batched) as b2:
+            assert b2.plan()[:2] == (depth, mult)
+        monkeypatch.setenv("CUPIC_BATCH_TUNE", "0")
+        with cg.Batch(batched) as b3:
+            assert b3.plan()[:2] == (4, 1)
+    finally:
+        for s in alone + batched:
+            s.close()
