@@ -1,15 +1,19 @@
-"""2000 steps of the 64x256 workload against the FP64 oracle: the
+"""The 64x256 workload's 1000 steps against the FP64 oracle: the
 time-averaged probe current and density profile within 2%.
 
 The workload as configured (Jacobi to max |dphi| < 1e-6, at most 2000
 sweeps a step) hits its sweep cap every step; the potential then lags the
 plasma and the run goes unstable near step 690, in the GPU and in both
-oracles alike.  The reference's own stop rule converges: max |dphi| < 1e-4
-(main.cu:64) after at least max(nnx, nny) sweeps (mesh.cu:67).  The
+oracles alike.  The reference's own stop rule converges further: max |dphi|
+< 1e-4 (main.cu:64) after at least max(nnx, nny) sweeps (mesh.cu:67).  The
 precision form states it as an FP64 residual below 4e-4 (a Jacobi sweep
 changes a node by a quarter of its residual), checked every 32 sweeps, after
 at least 288 sweeps (the multiple of 32 above max(nnx, nny) = 257) and at
-most 6016.  With that rule the run stays bounded for 2000 steps.
+most 6016.  With that rule the workload's 1000 steps run bounded; near step
+1100 the 6016-sweep cap no longer brings the residual below the tolerance,
+and by step 1155 electrons cross two rows a step -- in the FP64 oracle too,
+so 2000 steps of this shape are not run (the 2000-step check runs on a
+256x64 slab in test_gpu_precision.py).
 
 The GPU runs the precision form: FP32 sweeps on a correction, an FP64
 residual and update every 32 sweeps.  The oracle runs all-FP64 Jacobi with
@@ -27,7 +31,7 @@ from oracle.oracle import Oracle
 
 pytestmark = pytest.mark.gpu
 
-STEPS = 2000
+STEPS = 1000
 TOL = 0.02
 
 
@@ -71,7 +75,7 @@ def run_oracle(p):
     return np.array(cur), np.mean(np.array(dens, dtype=float), axis=0), flags
 
 
-def test_precision_form_2000_steps_against_fp64_oracle(gpu_lib):
+def test_precision_form_1000_steps_against_fp64_oracle(gpu_lib):
     p = params()
     g_cur, g_dens, g_sweeps, g_flags = run_gpu(p)
     o_cur, o_dens, o_flags = run_oracle(p)
