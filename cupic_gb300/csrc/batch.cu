@@ -67,8 +67,9 @@ struct cupic_batch {
   size_t nflags = 0, jsmem = 0;
   cudaGraphExec_t graph = nullptr;
   bool graph_ok = false;
-  // the batched solve's layout knobs in use: halo depth cap, CTA multiple
-  int knob_depth = 4, knob_mult = 1;
+  // the batched solve's layout knobs in use: halo depth cap, CTA multiple;
+  // tuned_n: the member count they were tuned for (0: not tuned)
+  int knob_depth = 4, knob_mult = 1, tuned_n = 0;
 };
 
 namespace {
@@ -355,7 +356,10 @@ int time_solve(cupic_batch *b, float *ms) {
 // tuning.  The epoch base of the halo words keeps advancing, as the
 // exchange protocol needs.  Picks are cached per process by the members'
 // multiset of (mesh shape, sweeps), and batches of fewer than kTuneMembers
-// members take the default knobs.  CUPIC_BATCH_TUNE=0 turns tuning off.
+// members take the default knobs.  A batch whose members change (a server
+// admitting and retiring requests) keeps its tuned knobs until its member
+// count doubles or halves, so that membership changes do not tune again.
+// CUPIC_BATCH_TUNE=0 turns tuning off.
 struct MixKey {
   std::vector<std::tuple<int, int, int, int>> shapes;
   bool operator<(const MixKey &o) const { return shapes < o.shapes; }
@@ -367,6 +371,10 @@ int tune_solve(cupic_batch *b) {
   const int n = (int)b->members.size();
   const char *env = getenv("CUPIC_BATCH_TUNE");
   if (n < kTuneMembers || (env && atoi(env) == 0)) return layout_solve(b, kDefaultKnobs);
+  if (b->tuned_n && n < 2 * b->tuned_n && 2 * n > b->tuned_n &&
+      layout_solve(b, Knobs{b->knob_depth, b->knob_mult}) == CUPIC_OK)
+    return CUPIC_OK;
+  b->tuned_n = n;
   MixKey key;
   for (const cupic_ctx *c : b->members)
     key.shapes.emplace_back(c->a.nnx, c->a.nny, c->p.max_sweeps, c->p.check_every);

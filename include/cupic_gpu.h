@@ -331,8 +331,9 @@ int cupic_batch_sync(cupic_batch *b);
  * 2, 4, 8 x CTA multiple 1, 2) on the members' own meshes -- saving and
  * restoring their potential, field and solver status -- and keeps the
  * fastest; picks are cached per process by the members' mesh shapes and
- * sweep counts.  Smaller sets, or CUPIC_BATCH_TUNE=0, take depth cap 4 and
- * multiple 1. */
+ * sweep counts, and a batch keeps its pick while its member count stays
+ * within a factor of two of the count it was tuned for.  Smaller sets, or
+ * CUPIC_BATCH_TUNE=0, take depth cap 4 and multiple 1. */
 int cupic_batch_plan(cupic_batch *b, int32_t *depth_cap, int32_t *cta_mult, int32_t *ctas);
 int cupic_batch_destroy(cupic_batch *b);
 
