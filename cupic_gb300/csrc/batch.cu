@@ -70,6 +70,10 @@ struct cupic_batch {
   // the batched solve's layout knobs in use: halo depth cap, CTA multiple;
   // tuned_n: the member count they were tuned for (0: not tuned)
   int knob_depth = 4, knob_mult = 1, tuned_n = 0;
+  // batched steps since d_halo was last zeroed: a halo word's epoch holds
+  // the solve count in 16 bits, so the words are zeroed before it can wrap
+  int64_t epoch_steps = 0;
+  size_t nhalo = 0;
 };
 
 namespace {
@@ -272,6 +276,8 @@ int layout_solve(cupic_batch *b, const Knobs &kn) {
     return rc;
   // a region may hold another instance's words with a matching epoch
   CU(cudaMemsetAsync(b->d_halo, 0, sizeof(unsigned long long) * nhalo, b->stream));
+  b->nhalo = nhalo;
+  b->epoch_steps = 0;
   b->nflags = nflags;
   std::vector<JacobiArgs> jargs(n);
   size_t of = 0, orr = 0, oh = 0;
@@ -605,6 +611,10 @@ int cupic_batch_step(cupic_batch *b, int32_t nsteps) {
     if (rc) return rc;
   }
   for (int s = 0; s < nsteps; ++s) {
+    if (++b->epoch_steps > 65000) {  // before the members' solve counts can wrap
+      CU(cudaMemsetAsync(b->d_halo, 0, sizeof(unsigned long long) * b->nhalo, b->stream));
+      b->epoch_steps = 1;
+    }
     if (b->graph_ok) {
       CU(cudaGraphLaunch(b->graph, b->stream));
     } else {

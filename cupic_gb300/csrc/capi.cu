@@ -309,9 +309,34 @@ int alloc_jacobi_scratch(cupic_ctx *c, int G, long long GK, int P) {
   CU(dalloc(c, &c->jflags, (size_t)G + 1));
   CU(dalloc(c, &c->jres, (size_t)2 * G));
   CU(dalloc(c, &c->jhalo, (size_t)4 * GK * P));
+  c->jhalo_words = (size_t)4 * GK * P;
   // epoch 0 is never valid; the solves on the context's stream follow the clearing
-  CU(cudaMemsetAsync(c->jhalo, 0, sizeof(unsigned long long) * 4 * (size_t)GK * P, c->stream));
+  CU(cudaMemsetAsync(c->jhalo, 0, sizeof(unsigned long long) * c->jhalo_words, c->stream));
+  c->epoch_solves = 0;
   return CUPIC_OK;
+}
+
+// A halo word carries the epoch (solve count << 16) + exchange index in 32
+// bits, so the solve count wraps every 65,536 solves.  A slot that the
+// solves since stopped rewriting (tolerance-stopped solves end after
+// different numbers of exchanges) could then hold a word whose epoch matches
+// again.  Before `solves` more solves are enqueued, the halo words are
+// zeroed (epoch 0 never matches) whenever the count since the last clearing
+// would reach kEpochGuard, ordered on the context's stream before them.
+constexpr int64_t kEpochGuard = 65000;
+int epoch_guard(cupic_ctx *c, int64_t solves) {
+  if (c->jhalo && c->epoch_solves + solves > kEpochGuard) {
+    CU(cudaMemsetAsync(c->jhalo, 0, sizeof(unsigned long long) * c->jhalo_words, c->stream));
+    c->epoch_solves = 0;
+  }
+  c->epoch_solves += solves;
+  return CUPIC_OK;
+}
+
+// solves (Jacobi launches) one solve of at most mx sweeps enqueues
+int64_t solves_of(const cupic_ctx *c, int mx) {
+  const int m = c->p.refine_every;
+  return m > 0 ? 1 + (std::max(mx, 0) + m - 1) / m : 1;
 }
 
 int set_jacobi_plan(cupic_ctx *c, int G, int B, int K, int P) {
@@ -733,6 +758,8 @@ int launch_steps(cupic_ctx *c, int64_t n) {
     if (rc) return rc;
   }
   for (int64_t i = 0; i < n; ++i) {
+    int rc = epoch_guard(c, solves_of(c, c->p.max_sweeps));
+    if (rc) return rc;
     if (c->graph_ok) {
       CU(cudaGraphLaunch(c->graph, c->stream));
     } else {
@@ -1213,7 +1240,8 @@ int init_plasma_enqueue(cupic_ctx *c) {
   rc = deposit_current(c);
   if (rc) return rc;
   const cupic_params &p = c->p;
-  rc = run_solve(c, p.init_tol, p.init_min_sweeps, p.init_max_sweeps, p.check_every, 1);
+  rc = epoch_guard(c, solves_of(c, p.init_max_sweeps));
+  if (!rc) rc = run_solve(c, p.init_tol, p.init_min_sweeps, p.init_max_sweeps, p.check_every, 1);
   if (rc) return rc;
   CU(launch_leapfrog_start(c->a, c->stream));
   rc = cupic_set_time(c, (int64_t)p.n_ini + 1, p.n_ini * p.dt + p.dt, -1.0, -1.0);
@@ -1285,7 +1313,8 @@ int cupic_init_mesh(cupic_ctx *c) {
   rc = deposit_current(c);
   if (rc) return rc;
   const cupic_params &p = c->p;
-  rc = run_solve(c, p.init_tol, p.init_min_sweeps, p.init_max_sweeps, p.check_every, 1);
+  rc = epoch_guard(c, solves_of(c, p.init_max_sweeps));
+  if (!rc) rc = run_solve(c, p.init_tol, p.init_min_sweeps, p.init_max_sweeps, p.check_every, 1);
   if (rc) return rc;
   rc = sync_check(c);
   if (rc) return rc;
@@ -1395,7 +1424,8 @@ int cupic_poisson_solver(cupic_ctx *c, double max_error, int32_t mn, int32_t mx,
     chk = c->p.check_every;
   }
   if (mx < 0) return CUPIC_ERR_ARG;
-  int rc = run_solve(c, max_error, mn, mx, chk, 0);
+  int rc = epoch_guard(c, solves_of(c, mx));
+  if (!rc) rc = run_solve(c, max_error, mn, mx, chk, 0);
   if (rc) return rc;
   return finish(c);
 }
@@ -1408,6 +1438,8 @@ int cupic_field_solver(cupic_ctx *c) {
   } else {
     JacobiArgs J = jargs(c, 0.0, 0, 0, 1, 1);
     J.write_stats = 0;
+    int rc = epoch_guard(c, 1);
+    if (rc) return rc;
     CU(launch_jacobi(c->a, J, c->stream));
   }
   return finish(c);
@@ -1488,7 +1520,8 @@ int cupic_step(cupic_ctx *c, int32_t nsteps) {
     // the solve reads its residual norm on the host: no graph, and a step
     // that runs out of room is completed before the next one starts
     for (int i = 0; i < nsteps; ++i) {
-      int rc = enqueue_step(c);
+      int rc = epoch_guard(c, solves_of(c, c->p.max_sweeps));
+      if (!rc) rc = enqueue_step(c);
       if (!rc) c->host_cur ^= 1;
       if (!rc) rc = settle(c);
       if (rc) return rc;
@@ -1558,7 +1591,8 @@ int cupic_step_timed(cupic_ctx *c, int32_t nsteps, float *phase_ms, int32_t npha
     if (cudaEventCreate(&e) != cudaSuccess) rc = CUPIC_ERR_CUDA;
   cudaError_t e = rc ? cudaErrorUnknown : cudaEventRecord(ev[0], c->stream);
   for (int s = 0; s < nsteps && e == cudaSuccess && !rc; ++s) {
-    rc = enqueue_step(c, &ev[(size_t)s * per + 1]);
+    rc = epoch_guard(c, solves_of(c, c->p.max_sweeps));
+    if (!rc) rc = enqueue_step(c, &ev[(size_t)s * per + 1]);
     if (!rc) c->host_cur ^= 1;
   }
   if (e == cudaSuccess && !rc) e = cudaStreamSynchronize(c->stream);

@@ -30,6 +30,9 @@ struct cupic_ctx {
   unsigned *jflags = nullptr;  // [G+1]: per-CTA sweep counters, then the barrier
   float *jres = nullptr;
   unsigned long long *jhalo = nullptr;  // halo words, zeroed at allocation
+  size_t jhalo_words = 0;
+  // solves enqueued since the halo words were last zeroed (see epoch_guard)
+  int64_t epoch_solves = 0;
   // precision form of the solve (refine_every > 0): FP64 potential, FP32
   // residual source and correction, the residual's max norm
   double *phi64 = nullptr;

@@ -37,8 +37,14 @@ static __device__ __align__(256) unsigned char g_solver_scratch[kStaticScratchBy
 std::mutex g_mu;
 constexpr int kMaxDevices = 64;
 void *g_scratch_addr[kMaxDevices] = {};
+// calls since the array's halo words were last zeroed, per device: a halo
+// word's epoch holds the solve count in 16 bits, so the words are zeroed
+// before the count can wrap (epoch 0 never matches)
+long long g_calls[kMaxDevices] = {};
 
-int scratch_for_current_device(unsigned char **out) {
+// the array's device address on the current device; *clear: the call must
+// zero the halo words first
+int scratch_for_current_device(unsigned char **out, bool *clear) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return CUPIC_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_mu);
@@ -50,6 +56,8 @@ int scratch_for_current_device(unsigned char **out) {
     }
     g_scratch_addr[dev] = ptr;
   }
+  *clear = ++g_calls[dev] > 65000;
+  if (*clear) g_calls[dev] = 1;
   *out = static_cast<unsigned char *>(g_scratch_addr[dev]);
   return CUPIC_OK;
 }
@@ -70,7 +78,8 @@ extern "C" int cupic_poisson_solver_static(const cupic_params *p, const int64_t 
   if (p->ncx < 2 || p->ncy < 2 || p->ncx > 4096 || !(p->ds > 0) || !(p->eps0 > 0))
     return CUPIC_ERR_ARG;
   unsigned char *scratch = nullptr;
-  int rc = scratch_for_current_device(&scratch);
+  bool clear_halo = false;
+  int rc = scratch_for_current_device(&scratch, &clear_halo);
   if (rc) return rc;
   int dev = 0, num_sms = 0, dev_max = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
@@ -165,6 +174,9 @@ extern "C" int cupic_poisson_solver_static(const cupic_params *p, const int64_t 
   // keeps the halo words of earlier calls from matching; launch_jacobi
   // clears the counters
   if (cudaMemsetAsync(ctl, 0, offsetof(Ctl, jepoch), st) != cudaSuccess) return CUPIC_ERR_CUDA;
+  if (clear_halo && cudaMemsetAsync(scratch + kCtlHeadBytes, 0, kStaticScratchBytes - kCtlHeadBytes, st) !=
+                        cudaSuccess)
+    return CUPIC_ERR_CUDA;
   if (launch_jacobi(a, J, st) != cudaSuccess) return CUPIC_ERR_CUDA;
   struct {
     uint32_t step_flags;

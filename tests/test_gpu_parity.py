@@ -325,3 +325,29 @@ def test_dense_cell_folds_its_charge_moments(make_pair):
     sim.cc(t)
     ora.inject(t)
     check_state(sim, ora)
+
+
+def test_solves_past_the_epoch_wrap_keep_the_oracle_bits(make_pair, monkeypatch):
+    """A halo word tags its value with the solve count in 16 bits, which
+    wraps every 65,536 solves; the library zeroes the words before that.
+    65,100 short multi-CTA solves with varying sweep counts (so varying
+    numbers of halo exchanges), each from a fresh potential, keep giving the
+    oracle's potential bit for bit, across the clearing."""
+    monkeypatch.setenv("CUPIC_JACOBI_DEPTH", "2")
+    sim, ora = make_pair("tiny", ctas=4)
+    sim.init_plasma()
+    ora.init_plasma()
+    base = ora.phi()
+    rng = np.random.default_rng(9)
+    for k in range(65100):
+        n = 2 + k % 5
+        if k % 1000 == 0 or k >= 64990:
+            phi0 = base + 1e-3 * rng.standard_normal(base.shape)
+            phi0[:, -1] = phi0[:, 0]
+            phi0 = phi0.astype(np.float32).astype(np.float64)
+            sim.set_phi(phi0)
+            ora.set_phi(phi0)
+        sim.poisson_solver(1e-30, n, n, n)
+        if k % 1000 == 0 or k >= 64990:
+            ora.solve(1e-30, n, n, n)
+            np.testing.assert_array_equal(sim.phi().astype(np.float64), ora.phi(), err_msg=f"solve {k}")
