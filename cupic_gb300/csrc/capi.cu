@@ -585,12 +585,15 @@ int refine_solve(cupic_ctx *c, double tol, int mn, int mx, int field, int write_
 }
 
 // The same solve with the stop test on the device: every correction of the
-// sweep cap is enqueued (residual, test, m sweeps, update), and once the
-// test has passed the remaining kernels return at once.  Nothing waits on
-// the host, so a step in the precision form is captured as one graph.  The
-// kernels, their order and their operands are those of refine_solve, so
-// the results are identical.  Caps needing more than kDeviceCorrections
-// corrections use refine_solve.
+// sweep cap is enqueued, and once the test has passed the remaining ones
+// return at once.  Nothing waits on the host, so a step in the precision
+// form is captured as one graph.  Each correction is one Jacobi launch with
+// the residual, the test and the update fused in (JacobiArgs::r64_phi): the
+// operations and their order are those of refine_solve's separate kernels,
+// so the results are identical, with three launches and two passes over
+// the FP64 potential fewer per correction.  A last launch without sweeps
+// tests the residual after the final correction.  Caps needing more than
+// kDeviceCorrections corrections use refine_solve.
 constexpr int kDeviceCorrections = 512;
 
 bool refine_on_device(const cupic_ctx *c, int mx) {
@@ -603,18 +606,21 @@ int refine_solve_device(cupic_ctx *c, double tol, int mn, int mx, int field, int
   CU(cudaMemsetAsync(&c->ctl->refine_done, 0, sizeof(int32_t), c->stream));
   CU(launch_r64_source(c->a, c->b64, c->stream));
   for (int sweeps = 0;;) {
-    CU(launch_r64_residual(c->a, c->phi64, c->b64, c->rr, c->maxr, c->stream, 1));
-    CU(launch_r64_decide(c->a, c->maxr, sweeps, mn, mx, tol, write_stats, c->stream));
-    if (sweeps >= mx) break;
-    const int k = std::min(m, mx - sweeps);
-    JacobiArgs J = jargs(c, 0.0, k, k, k, 0);
+    const int k = sweeps >= mx ? 0 : std::min(m, mx - sweeps);
+    JacobiArgs J = jargs(c, 0.0, k, k, std::max(k, 1), 0);
     J.write_stats = 0;
     J.phi = c->dl;  // the correction starts from zero
     J.phi_zero = 1;
-    J.src = c->rr;
     J.gated = 1;
+    J.r64_phi = c->phi64;
+    J.r64_b = c->b64;
+    J.r64_tol = tol;
+    J.r64_done = sweeps;
+    J.r64_mn = mn;
+    J.r64_mx = mx;
+    J.r64_stats = write_stats;
     CU(launch_jacobi(c->a, J, c->stream));
-    CU(launch_r64_update(c->a, c->phi64, c->dl, c->stream, 1));
+    if (sweeps >= mx) break;
     sweeps += k;
   }
   // the FP32 potential (and the field) from phi64

@@ -104,6 +104,19 @@ struct JacobiArgs {
   unsigned long long *halo;  // [2 parity][G][2 sides][depth rows][pitch] {value, epoch} words
   float *phi;             // the potential solved for; NULL: a.phi
   const float *src;       // FP32 source per node; NULL: the charge accumulator a.rho[cur]
+  // A correction of the precision form with its residual, stop test and
+  // update fused in (r64_phi != NULL; phi is the correction, phi_zero set,
+  // no convergence checks): the kernel forms the FP64 residual
+  // r = b - A phi64 of its rows as its FP32 source, takes the max norm over
+  // the grid, and applies the stop test of the solve (after r64_done
+  // correction sweeps: stop when r64_done >= r64_mn and max |r| < r64_tol,
+  // or r64_done >= r64_mx; the stopping test sets ctl->refine_done and, with
+  // r64_stats, records the sweeps and the residual).  If it goes on, it runs
+  // its sweeps and adds the correction to phi64 on its owned rows.
+  double *r64_phi;
+  const double *r64_b;
+  double r64_tol;
+  int32_t r64_done, r64_mn, r64_mx, r64_stats;
 };
 
 // a group of CTAs of the batched solve and its instances (list[begin..end))

@@ -73,6 +73,24 @@ __device__ __forceinline__ float block_max(float v, float *red) {
   return red[32];
 }
 
+// block max of non-negative doubles (their bit patterns order as unsigned
+// 64-bit integers); every thread gets the result
+__device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v,
+                                                            unsigned long long *red) {
+  for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_down_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  if (warp == 0) {
+    unsigned long long w = lane < (int)(blockDim.x >> 5) ? red[lane] : 0ull;
+    for (int o = 16; o > 0; o >>= 1) w = max(w, __shfl_down_sync(0xffffffffu, w, o));
+    if (lane == 0) red[32] = w;
+  }
+  __syncthreads();
+  return red[32];
+}
+
 }  // namespace
 
 struct SweepGeom {
@@ -338,7 +356,11 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
   }
   // Load the buffered rows: the (row, column) pairs taken kLoadBatch at a
   // time per thread with all their loads issued before the first store, so
-  // a batch costs one memory round trip instead of one per row.
+  // a batch costs one memory round trip instead of one per row.  A fused
+  // correction forms its source here: the FP64 residual of the node, in the
+  // operation order of k_r64_residual (refine.cu), rounded to FP32 once; the
+  // max |r| over the CTA's owned rows feeds the stop test.
+  double rmax = 0.0;
   {
     const int total = nrows * nnx;
     for (int k0 = tid; k0 < total; k0 += kJBlock * kLoadBatch) {
@@ -353,7 +375,17 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
           const size_t rb = (size_t)j * nnx;
           v[u] = J.phi_zero ? 0.0f : phi[rb + i];
           if (j >= 1 && j <= nny - 2) {
-            if (J.src) {
+            if (J.r64_phi) {
+              const double *q = J.r64_phi;
+              const int ii = i == nnx - 1 ? 0 : i;  // the mirror column carries column 0's residual
+              const double cc = q[rb + ii];
+              const double w = q[rb + (ii == 0 ? nnx - 2 : ii - 1)];
+              const double e = q[rb + ii + 1];
+              const double n = q[rb + nnx + ii], so = q[rb - nnx + ii];
+              const double r = J.r64_b[rb + ii] - (4.0 * cc - (((w + e) + n) + so));
+              bv[u] = __double2float_rn(r);
+              if (j >= r0 && j < r1) rmax = fmax(rmax, fabs(r));
+            } else if (J.src) {
               bv[u] = J.src[rb + i];
             } else {
               const long long f = (i == 0 || i == nnx - 1) ? acc[rb] + acc[rb + nnx - 1] : acc[rb + i];
@@ -375,6 +407,42 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
     }
   }
   __syncthreads();
+
+  // a fused correction: the stop test of the solve on the grid's max |r|
+  int chk0 = 0;  // rounds of the grid barrier counter used so far
+  if (J.r64_phi) {
+    __shared__ unsigned long long red64[33];
+    unsigned long long gm = block_max_u64((unsigned long long)__double_as_longlong(rmax), red64);
+    if (G > 1) {
+      // the CTAs' maxima in the residual slots, read back after a grid
+      // barrier (a fused correction runs no convergence checks, which use
+      // the same slots)
+      unsigned long long *slots = reinterpret_cast<unsigned long long *>(J.res_cta);
+      if (tid == 0) {
+        __stcg(&slots[c], gm);
+        __threadfence();
+        atomicAdd(J.bar, 1u);
+        if (!wait_geq(J.bar, (unsigned)G, ctl)) bail = 1;
+      }
+      __syncthreads();
+      if (bail) return;
+      unsigned long long m = 0ull;
+      for (int k = tid; k < G; k += kJBlock) m = max(m, __ldcg(&slots[k]));
+      gm = block_max_u64(m, red64);
+      chk0 = 1;
+    }
+    const double res = __longlong_as_double((long long)gm);
+    if ((J.r64_done >= J.r64_mn && res < J.r64_tol) || J.r64_done >= J.r64_mx) {
+      if (c == 0 && tid == 0) {
+        ctl->refine_done = 1;
+        if (J.r64_stats) {
+          ctl->sweeps = J.r64_done;
+          ctl->residual = (float)res;
+        }
+      }
+      return;  // no sweeps, so no halo words of this solve's epochs
+    }
+  }
 
   const int W = nnx - 1;  // computed columns 0 .. nnx-2; column nnx-1 mirrors 0
   const int o0 = r0 - lo, o1 = r1 - lo;  // owned local rows
@@ -504,7 +572,7 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
     return true;
   };
 
-  int src = 0, done = 0, nchk = 0, m = 0, pending = 0, to_check = J.check_every;
+  int src = 0, done = 0, nchk = chk0, m = 0, pending = 0, to_check = J.check_every;
   float last = INFINITY;
   for (int s = 1; s <= J.max_sweeps; ++s) {
     float *S = src ? buf1 : buf0;
@@ -583,8 +651,17 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
   // write back the owned rows; derive E = -grad phi (mesh.cu:413-468).  The
   // rows r0-1 and r1 are current: either just exchanged or updated in the
   // last sweep of an unfinished temporal block.
-  for (int lr = o0; lr < o1; ++lr)
-    for (int i = tid; i < nnx; i += kJBlock) phi[(size_t)(lo + lr) * nnx + i] = F[lr * P + i];
+  if (J.r64_phi) {
+    // a fused correction: phi64 += correction on the owned rows (every
+    // column, the mirror included, as k_r64_update does)
+    if (done > 0)
+      for (int lr = o0; lr < o1; ++lr)
+        for (int i = tid; i < nnx; i += kJBlock)
+          J.r64_phi[(size_t)(lo + lr) * nnx + i] += (double)F[lr * P + i];
+  } else {
+    for (int lr = o0; lr < o1; ++lr)
+      for (int i = tid; i < nnx; i += kJBlock) phi[(size_t)(lo + lr) * nnx + i] = F[lr * P + i];
+  }
   if (J.do_field) {
     for (int lr = o0; lr < o1; ++lr) {
       const float *cr = F + lr * P;

@@ -144,3 +144,37 @@ def test_probe_current_and_density_within_2pct_of_fp64(sims):
           f"diff {abs(ig - io) / io:.4f}; density profile max deviation {dev:.4f} of bulk")
     assert abs(ig - io) <= 0.02 * io
     assert dev <= 0.02
+
+
+def test_precision_form_with_many_ctas_matches_oracle_bit_for_bit(sims, monkeypatch):
+    """The 64x256 workload in the precision form with the reference's stop
+    rule (FP64 residual below 4e-4 after at least 288 sweeps, at most 6016),
+    its correction solves split over 8 CTAs that trade halo rows: 20 steps
+    give the FP32 oracle's particles, FP64 potential, field, sweep counts and
+    residuals bit for bit."""
+    monkeypatch.setenv("CUPIC_JACOBI_CTAS", "8")
+    monkeypatch.setenv("CUPIC_JACOBI_DEPTH", "4")
+    p = cg.workload_params("small", refine_every=32, tol=4e-4, min_sweeps=288, max_sweeps=6016,
+                           check_every=32, init_tol=4e-3, init_min_sweeps=288,
+                           init_max_sweeps=20000)
+    sim = cg.Sim(p)
+    sims.append(sim)
+    assert sim.solver_plan()[0] == 8
+    ora = Oracle(p, fp64=False)
+    sim.init_plasma()
+    ora.init_plasma()
+    np.testing.assert_array_equal(sim.phi64(), ora.phi())
+    for _ in range(4):
+        sim.step(5)
+        ora.step(5)
+        for g, o in zip(sim.stats(1), [ora.stats()]):
+            for k in ("absorbed", "removed", "injected", "live", "sweeps"):
+                assert g[k] == o[k], k
+            assert g["residual"] == o["residual"]
+    for sp in (0, 1):
+        np.testing.assert_array_equal(sim.particles(sp), ora.particles(sp))
+    np.testing.assert_array_equal(sim.phi64(), ora.phi())
+    exg, eyg = sim.efield()
+    exo, eyo = ora.efield()
+    np.testing.assert_array_equal(exg.astype(np.float64), exo)
+    np.testing.assert_array_equal(eyg.astype(np.float64), eyo)
