@@ -48,14 +48,14 @@ KERNELS_PER_STEP = 8
 
 def kernels_per_step(p):
     """Kernels one step launches.  The precision form replaces the solve by
-    the FP64 source, per correction up to the sweep cap a residual, a stop
-    test, a Jacobi launch and an update (the ones after the stop test return
-    at once), a last residual and test, and the field; its step also clears
-    the next charge with its own kernel."""
+    the FP64 source, one Jacobi launch per correction up to the sweep cap
+    (each with the residual, the stop test and the update fused in; the
+    ones after the stop test return at once), a last test launch and the
+    field; its step also clears the next charge with its own kernel."""
     if p.refine_every <= 0:
         return KERNELS_PER_STEP
     corrections = -(-max(p.max_sweeps, 0) // p.refine_every)
-    return (KERNELS_PER_STEP - 1) + 1 + 1 + 4 * corrections + 2 + 1
+    return (KERNELS_PER_STEP - 1) + 1 + 1 + corrections + 1 + 1
 
 # algorithmic bytes per unit of work (FP32 SoA, 16 B state per particle)
 PUSH_BYTES_PER_PARTICLE = 32      # 16 B read + 16 B write
