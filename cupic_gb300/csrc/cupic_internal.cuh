@@ -272,6 +272,28 @@ __device__ __forceinline__ void gather_tile(const SimArgs &a, const float2 *tile
   Epy = e.y;
 }
 
+// The same gather from a tile of node pairs: entry i of a row holds nodes
+// i and i+1 of that row as {Ex_i, Ey_i, Ex_i+1, Ey_i+1}, rows of nnx-1
+// entries, so a particle reads its four nodes with two 16-byte loads.  The
+// values and the order of operations are those of gather_tile.
+__device__ __forceinline__ void gather_pairs(const SimArgs &a, const float4 *tile, float x, float y,
+                                             int s, float &Epx, float &Epy) {
+  const float2 sxy = __fmul2_rn(make_float2(x, y), make_float2(a.inv_ds, a.inv_ds));
+  const int ic = cfloorf(sxy.x, 0, a.ncx - 1);
+  const float2 d = __fadd2_rn(sxy, make_float2(-(float)ic, -(float)s));  // sx - ic, sy - s
+  const float fx = clamp01f(d.x), fy = clamp01f(d.y);
+  const float2 g = __fadd2_rn(make_float2(1.0f, 1.0f), make_float2(-fx, -fy));  // gx, gy
+  const float2 wlo = __fmul2_rn(make_float2(g.x, fx), make_float2(g.y, g.y));    // w00, w10
+  const float2 whi = __fmul2_rn(make_float2(g.x, fx), make_float2(fy, fy));      // w01, w11
+  const float4 lo = tile[ic], hi = tile[a.ncx + ic];
+  float2 e = __fmul2_rn(make_float2(wlo.x, wlo.x), make_float2(lo.x, lo.y));
+  e = __ffma2_rn(make_float2(wlo.y, wlo.y), make_float2(lo.z, lo.w), e);
+  e = __ffma2_rn(make_float2(whi.x, whi.x), make_float2(hi.x, hi.y), e);
+  e = __ffma2_rn(make_float2(whi.y, whi.y), make_float2(hi.z, hi.w), e);
+  Epx = e.x;
+  Epy = e.y;
+}
+
 // fixed-point CIC weights: kFixBits = 18 fractional bits per axis and the
 // cross term FX*FY rounded to a multiple of 2^(32-18), so the four weights
 // are exact integers that sum to 2^32 per particle.  18 bits put the

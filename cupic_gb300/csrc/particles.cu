@@ -334,7 +334,7 @@ __device__ __forceinline__ uint32_t field2(uint32_t v) { return v >> 21; }
 
 size_t push_smem_bytes(int nnx, int pb) {
   return (size_t)kStages * pb * (pb == 256 ? 4 : 2) * sizeof(float4) + rho_moment_bytes(3, nnx - 1) +
-         (size_t)2 * nnx * sizeof(float2);
+         (size_t)2 * (nnx - 1) * sizeof(float4);
 }
 
 template <int PB>
@@ -352,8 +352,9 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
   const int nnx = a.nnx;
   const int ncx = a.ncx;
   float4 *stage = reinterpret_cast<float4 *>(push_raw);
-  float2 *etile = reinterpret_cast<float2 *>(stage + kStages * CH);  // node rows s, s+1
-  unsigned *tmom = reinterpret_cast<unsigned *>(etile + 2 * nnx);      // cell rows s-1..s+1
+  // node rows s, s+1 as node pairs (gather_pairs): 2 x ncx entries
+  float4 *etile = stage + kStages * CH;
+  unsigned *tmom = reinterpret_cast<unsigned *>(etile + 2 * ncx);  // cell rows s-1..s+1
   __shared__ __align__(8) uint64_t full[kStages];
   __shared__ uint2 wmask[2][NE];  // per-entry category ballots, alternate chunks
   __shared__ unsigned long long s_cnt[2];
@@ -380,7 +381,12 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
   }
   RhoMoments T{tmom, s - 1, 3, ncx, nnx, a.nny, a.rho[ctl->cur ^ 1]};
   T.zero();
-  for (int k = tid; k < 2 * nnx; k += PB) etile[k] = a.E[(size_t)s * nnx + k];
+  for (int k = tid; k < 2 * ncx; k += PB) {
+    const int r = k >= ncx ? 1 : 0, i = k - r * ncx;
+    const float2 *er = a.E + (size_t)(s + r) * nnx + i;
+    const float2 e0 = er[0], e1 = er[1];
+    etile[k] = make_float4(e0.x, e0.y, e1.x, e1.y);
+  }
   __syncthreads();
 
   uint32_t fl = 0;
@@ -404,7 +410,7 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
       if (idx < cnt) {
         float4 v = stage[st * CH + idx];
         float ex, ey;
-        gather_tile(a, etile, v.x, v.y, s, ex, ey);
+        gather_pairs(a, etile, v.x, v.y, s, ex, ey);
         // v += dtqm E, then r += dt v, both components per packed operation
         const float2 vel = __ffma2_rn(make_float2(dtqm, dtqm), make_float2(ex, ey), make_float2(v.z, v.w));
         const float2 pos = __ffma2_rn(make_float2(a.dt, a.dt), vel, make_float2(v.x, v.y));
