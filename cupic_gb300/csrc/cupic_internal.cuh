@@ -151,6 +151,16 @@ __device__ __forceinline__ int cfloord(double v, int lo, int hi) {
   return i > hi ? hi : i;
 }
 
+// Floor and nearest-even rounding of floats in [-0, 2^23) on the FP32 pipe
+// instead of the conversion unit: t = v + 2^23 rounded down (or to nearest
+// even) is exactly 2^23 + floor(v) (or rint(v)), whose bits less those of
+// 2^23 are that integer; 2^23 - t rounded down is minus it as a float,
+// exactly, with -0 for 0 (as -(float)0).
+constexpr float kMagic23 = 8388608.0f;
+constexpr int kMagic23Bits = 0x4B000000;
+__device__ __forceinline__ int magic_int(float t) { return __float_as_int(t) - kMagic23Bits; }
+__device__ __forceinline__ float neg_magic_float(float t) { return __fsub_rd(kMagic23, t); }
+
 __device__ __forceinline__ int row_of(const SimArgs &a, float y) {
   return cfloorf(__fmul_rn(y, a.inv_ds), 0, a.ncy - 1);
 }
@@ -279,8 +289,10 @@ __device__ __forceinline__ void gather_tile(const SimArgs &a, const float2 *tile
 __device__ __forceinline__ void gather_pairs(const SimArgs &a, const float4 *tile, float x, float y,
                                              int s, float &Epx, float &Epy) {
   const float2 sxy = __fmul2_rn(make_float2(x, y), make_float2(a.inv_ds, a.inv_ds));
-  const int ic = cfloorf(sxy.x, 0, a.ncx - 1);
-  const float2 d = __fadd2_rn(sxy, make_float2(-(float)ic, -(float)s));  // sx - ic, sy - s
+  // ic = floor(sx) clamped to [0, ncx-1] (NaN -> 0), as cfloorf
+  const float t = __fadd_rd(fminf(fmaxf(sxy.x, 0.0f), (float)(a.ncx - 1)), kMagic23);
+  const int ic = magic_int(t);
+  const float2 d = __fadd2_rn(sxy, make_float2(neg_magic_float(t), -(float)s));  // sx - ic, sy - s
   const float fx = clamp01f(d.x), fy = clamp01f(d.y);
   const float2 g = __fadd2_rn(make_float2(1.0f, 1.0f), make_float2(-fx, -fy));  // gx, gy
   const float2 wlo = __fmul2_rn(make_float2(g.x, fx), make_float2(g.y, g.y));    // w00, w10
@@ -323,19 +335,25 @@ __device__ __forceinline__ CicFixed cic_fixed(const SimArgs &a, float x, float y
   CicFixed r;
   const float2 sxy = __fmul2_rn(make_float2(x, y), make_float2(a.inv_ds, a.inv_ds));
   if (INSIDE) {
-    r.ic = min(__float2int_rd(sxy.x), a.ncx - 1);
-    r.jc = min(__float2int_rd(sxy.y), a.ncy - 1);
+    // sxy >= 0: floor of min(sxy, n-1) = min(floor(sxy), n-1), on the FP32 pipe
+    const float2 t = __fadd2_rd(make_float2(fminf(sxy.x, (float)(a.ncx - 1)), fminf(sxy.y, (float)(a.ncy - 1))),
+                                make_float2(kMagic23, kMagic23));
+    r.ic = magic_int(t.x);
+    r.jc = magic_int(t.y);
+    const float2 d = __fadd2_rn(sxy, __ffma2_rd(t, make_float2(-1.0f, -1.0f), make_float2(kMagic23, kMagic23)));
+    const float2 f = __fadd2_rn(__fmul2_rn(make_float2(fminf(d.x, 1.0f), fminf(d.y, 1.0f)),
+                                           make_float2(kFixOne, kFixOne)),
+                                make_float2(kMagic23, kMagic23));
+    r.FX = magic_int(f.x);
+    r.FY = magic_int(f.y);
   } else {
     r.ic = cfloorf(sxy.x, 0, a.ncx - 1);
     r.jc = cfloorf(sxy.y, 0, a.ncy - 1);
+    const float2 d = __fadd2_rn(sxy, make_float2(-(float)r.ic, -(float)r.jc));
+    const float2 f = __fmul2_rn(make_float2(clamp01f(d.x), clamp01f(d.y)), make_float2(kFixOne, kFixOne));
+    r.FX = __float2int_rn(f.x);
+    r.FY = __float2int_rn(f.y);
   }
-  const float2 d = __fadd2_rn(sxy, make_float2(-(float)r.ic, -(float)r.jc));
-  const float2 f = INSIDE ? __fmul2_rn(make_float2(fminf(d.x, 1.0f), fminf(d.y, 1.0f)),
-                                       make_float2(kFixOne, kFixOne))
-                          : __fmul2_rn(make_float2(clamp01f(d.x), clamp01f(d.y)),
-                                       make_float2(kFixOne, kFixOne));
-  r.FX = __float2int_rn(f.x);
-  r.FY = __float2int_rn(f.y);
   r.FXY = (int)(((unsigned long long)r.FX * (unsigned long long)r.FY +
                  (1ull << (kFixBits - 1))) >> kFixBits);
   return r;
