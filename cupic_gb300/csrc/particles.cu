@@ -14,6 +14,10 @@
 //   k_inject        draws the injected flux of the step (cc.cu:179-256),
 //                   appends it to the rows it falls in, deposits it
 //   k_finalize      per-step counters, clock advance, charge buffer flip
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "cupic_internal.cuh"
 #include "kernels.h"
 
@@ -72,6 +76,26 @@ struct RhoMoments {
       atomicAdd(&g[n00 + nnx], (unsigned long long)(q * c.w01()));
       atomicAdd(&g[n00 + nnx + 1], (unsigned long long)(q * c.w11()));
     }
+  }
+  // The common case without a branch: a particle inside the domain whose
+  // cell row is within one of row s (this tile's middle row, crow0 = s-1)
+  // adds its moments to the tile; returns its row step -1, 0 or 1, else 2
+  // (and deposits nothing).  Out-of-domain or non-finite positions give
+  // clamped in-range indices and no deposit.
+  __device__ __forceinline__ int deposit_near(const SimArgs &a, const float4 &v, int s, bool live) const {
+    const bool inside = v.y >= 0.0f && v.y < a.Ly && v.x >= 0.0f && v.x < a.Lx;
+    const CicFixed c = cic_fixed<true>(a, v.x, v.y);
+    const int dj = c.jc - s;
+    const bool near = live && inside && dj >= -1 && dj <= 1;
+    if (near) {
+      const int nc = cells();
+      unsigned *mc = m + ((dj + 1) * ncx + c.ic);
+      atomicAdd(mc, 1u);
+      atomicAdd(mc + nc, (unsigned)c.FX);
+      atomicAdd(mc + 2 * nc, (unsigned)c.FY);
+      atomicAdd(mc + 3 * nc, (unsigned)c.FXY);
+    }
+    return near ? dj : 2;
   }
   __device__ __forceinline__ void zero() const {
     for (int k = threadIdx.x; k < 4 * cells(); k += blockDim.x) m[k] = 0u;
@@ -134,21 +158,19 @@ __device__ __forceinline__ Cls classify(const SimArgs &a, const float4 &p, int s
   return {d, f};
 }
 
-// A pushed particle of row s: classify() and, if it stays in the row set,
-// deposit it; returns 0 stay, 1 up, 2 down, 3 absorbed or removed.
-// Fast path: x = wrap(x0 + dt vx) and y = y0 + dt vy are finite only if vx
-// and vy are (dt = 0 turns an infinite velocity into NaN), so a particle
-// with both coordinates inside the domain is finite4 and needs no further
-// test but the row step; its row is the deposit's cell row.
-__device__ __forceinline__ int settle(const SimArgs &a, const float4 &v, int s, const RhoMoments &T,
-                                      int q, uint32_t &fl, unsigned &nabs, unsigned &nrem) {
+// A pushed particle of row s, settled in two parts: RhoMoments::deposit_near()
+// takes the common case without a branch (inside the domain, a row step of
+// at most one), and settle_far() the rest: a row step beyond one (deposited
+// to global memory, CFL flag) or a position outside the domain (classify()).
+// Both return 0 stay, 1 up, 2 down, 3 absorbed or removed.  x = wrap(x0 +
+// dt vx) and y = y0 + dt vy are finite only if vx and vy are (dt = 0 turns
+// an infinite velocity into NaN), so a particle with both coordinates
+// inside the domain is finite4 and needs no further test but the row step;
+// its row is the deposit's cell row.
+__device__ __forceinline__ int settle_far(const SimArgs &a, const float4 &v, int s, const RhoMoments &T,
+                                          int q, uint32_t &fl, unsigned &nabs, unsigned &nrem) {
   if (v.y >= 0.0f && v.y < a.Ly && v.x >= 0.0f && v.x < a.Lx) {
-    const CicFixed c = cic_fixed<true>(a, v.x, v.y);
-    T.deposit(c, q);
-    const int dj = c.jc - s;  // c.jc == row_of(a, v.y)
-    if (dj == 0) return 0;
-    if (dj == 1) return 1;
-    if (dj == -1) return 2;
+    T.deposit(cic_fixed<true>(a, v.x, v.y), q);
     fl |= CUPIC_FLAG_CFL;
     return 0;
   }
@@ -164,6 +186,23 @@ __device__ __forceinline__ int settle(const SimArgs &a, const float4 &v, int s, 
   }
   T.deposit(a, v.x, v.y, q);
   return c.dest == s ? 0 : (c.dest == s + 1 ? 1 : 2);
+}
+
+// The same in one call, with a branch: the push kernels of 2 particles a
+// thread (the batched ones, held to 64 registers) run faster this way.
+__device__ __forceinline__ int settle(const SimArgs &a, const float4 &v, int s, const RhoMoments &T,
+                                      int q, uint32_t &fl, unsigned &nabs, unsigned &nrem) {
+  if (v.y >= 0.0f && v.y < a.Ly && v.x >= 0.0f && v.x < a.Lx) {
+    const CicFixed c = cic_fixed<true>(a, v.x, v.y);
+    T.deposit(c, q);
+    const int dj = c.jc - s;  // c.jc == row_of(a, v.y)
+    if (dj == 0) return 0;
+    if (dj == 1) return 1;
+    if (dj == -1) return 2;
+    fl |= CUPIC_FLAG_CFL;
+    return 0;
+  }
+  return settle_far(a, v, s, T, q, fl, nabs, nrem);
 }
 
 }  // namespace
@@ -337,7 +376,10 @@ size_t push_smem_bytes(int nnx, int pb) {
          (size_t)2 * (nnx - 1) * sizeof(float4);
 }
 
-template <int PB>
+// NEAR: the four particles of a thread settle their common case without a
+// branch (RhoMoments::deposit_near), the rest after (settle_far).  Their
+// chains then interleave, at 72 registers a thread instead of 64.
+template <int PB, bool NEAR = false>
 __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const int sp,
                                           unsigned char *push_raw) {
   constexpr int NW = PB / 32;
@@ -402,12 +444,16 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
     if (!mbar_wait(&full[st], (uint32_t)((k / kStages) & 1))) fl |= CUPIC_FLAG_TIMEOUT;
     const int cnt = min(CH, nn - k * CH);
     float4 p[kPPT];
-    int cat[kPPT];
+    int cat[kPPT];  // 0 stay, 1 up, 2 down, 3 none
+    if constexpr (NEAR) {
+      static_assert(kPPT == 4, "the branch-free form is written for four particles a thread");
+      bool rare = false;
 #pragma unroll
-    for (int j = 0; j < kPPT; ++j) {
-      const int idx = j * PB + tid;
-      cat[j] = 3;  // 0 stay, 1 up, 2 down, 3 none
-      if (idx < cnt) {
+      for (int j = 0; j < kPPT; ++j) {
+        const int idx = j * PB + tid;
+        const bool live = idx < cnt;
+        // a slot past the chunk's end computes on stale stage words: every
+        // index it forms is clamped in range, and it deposits and stores nothing
         float4 v = stage[st * CH + idx];
         float ex, ey;
         gather_pairs(a, etile, v.x, v.y, s, ex, ey);
@@ -415,8 +461,31 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
         const float2 vel = __ffma2_rn(make_float2(dtqm, dtqm), make_float2(ex, ey), make_float2(v.z, v.w));
         const float2 pos = __ffma2_rn(make_float2(a.dt, a.dt), vel, make_float2(v.x, v.y));
         v = make_float4(wrap_x(a, pos.x), pos.y, vel.x, vel.y);
-        cat[j] = settle(a, v, s, T, qc, fl, nabs, nrem);
+        const int dj = T.deposit_near(a, v, s, live);
+        cat[j] = dj == 0 ? 0 : (dj == 1 ? 1 : (dj == -1 ? 2 : 3));
+        rare |= live && cat[j] == 3;
         p[j] = v;
+      }
+      if (rare) {
+#pragma unroll
+        for (int j = 0; j < kPPT; ++j)
+          if (j * PB + tid < cnt && cat[j] == 3) cat[j] = settle_far(a, p[j], s, T, qc, fl, nabs, nrem);
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < kPPT; ++j) {
+        const int idx = j * PB + tid;
+        cat[j] = 3;
+        if (idx < cnt) {
+          float4 v = stage[st * CH + idx];
+          float ex, ey;
+          gather_pairs(a, etile, v.x, v.y, s, ex, ey);
+          const float2 vel = __ffma2_rn(make_float2(dtqm, dtqm), make_float2(ex, ey), make_float2(v.z, v.w));
+          const float2 pos = __ffma2_rn(make_float2(a.dt, a.dt), vel, make_float2(v.x, v.y));
+          v = make_float4(wrap_x(a, pos.x), pos.y, vel.x, vel.y);
+          cat[j] = settle(a, v, s, T, qc, fl, nabs, nrem);
+          p[j] = v;
+        }
       }
     }
     // category bits of the warp's lanes: 00 stay, 01 up, 10 down, 11 none
@@ -515,10 +584,22 @@ __device__ __forceinline__ void push_unit(const SimArgs &a, const int s, const i
 }
 
 // block 2s + sp pushes species sp of row s: both species of a row are
-// independent units of equal size, which halves the tail of the last wave
+// independent units of equal size, which halves the tail of the last wave.
+// Rows whose tiles leave room for 4 blocks per SM (up to about 300 cells)
+// take k_push_deposit_narrow, the branching settle at 64 registers, so
+// that 4 blocks fit; wider rows, held to 3 blocks by shared memory anyway,
+// take the branch-free settle at 72 registers (1.7% faster at 512 cells,
+// and 5% slower on the batched step's meshes of 128 and 256 cells, where it
+// costs the fourth block).  The narrow kernel keeps the bound of 3 blocks:
+// bounding it to 4 made the compiler take 61 registers and the batched
+// step 2.6% slower.
 __global__ void __launch_bounds__(kPB, 3) k_push_deposit(SimArgs a) {
   extern __shared__ __align__(128) unsigned char push_raw[];
-  push_unit<kPB>(a, blockIdx.x >> 1, blockIdx.x & 1, push_raw);
+  push_unit<kPB, true>(a, blockIdx.x >> 1, blockIdx.x & 1, push_raw);
+}
+__global__ void __launch_bounds__(kPB, 3) k_push_deposit_narrow(SimArgs a) {
+  extern __shared__ __align__(128) unsigned char push_raw[];
+  push_unit<kPB, false>(a, blockIdx.x >> 1, blockIdx.x & 1, push_raw);
 }
 
 // many contexts in one launch: block 2b + sp pushes species sp of work[b] =
@@ -526,7 +607,7 @@ __global__ void __launch_bounds__(kPB, 3) k_push_deposit(SimArgs a) {
 // row's unit is mostly set-up, which more resident blocks overlap), 512
 // otherwise
 template <int PB>
-__global__ void __launch_bounds__(PB, PB == 128 ? 8 : (PB == 256 ? 4 : 2))
+__global__ void __launch_bounds__(PB, PB == 128 ? 8 : 2)
     k_push_deposit_batch(const SimArgs *__restrict__ inst, const int2 *__restrict__ work) {
   extern __shared__ __align__(128) unsigned char push_raw[];
   // the instance's arguments in shared memory: read there as needed instead
@@ -945,13 +1026,47 @@ cudaError_t launch_leapfrog_start(const SimArgs &a, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+namespace {
+// whether k_push_deposit_narrow fits 4 blocks per SM with `bytes` of
+// dynamic shared memory on the current device (cached)
+cudaError_t push_narrow(size_t bytes, bool *narrow) {
+  static std::mutex mu;
+  static std::map<std::pair<int, size_t>, bool> memo;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_pair(dev, bytes);
+  const auto it = memo.find(key);
+  if (it != memo.end()) {
+    *narrow = it->second;
+    return cudaSuccess;
+  }
+  const void *fn = reinterpret_cast<const void *>(k_push_deposit_narrow);
+  e = raise_dyn_smem(fn, bytes);
+  int n = 0;
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_push_deposit_narrow, kPB, bytes);
+  if (e != cudaSuccess) return e;
+  *narrow = memo[key] = n >= 4;
+  return cudaSuccess;
+}
+}  // namespace
+
 cudaError_t push_set_smem(size_t bytes) {
-  return raise_dyn_smem(reinterpret_cast<const void *>(k_push_deposit), bytes);
+  bool narrow = false;
+  const cudaError_t e = raise_dyn_smem(reinterpret_cast<const void *>(k_push_deposit), bytes);
+  return e != cudaSuccess ? e : push_narrow(bytes, &narrow);
 }
 
 cudaError_t launch_push_deposit(const SimArgs &a, cudaStream_t st) {
   const size_t sm = push_smem_bytes(a.nnx, kPB);
-  k_push_deposit<<<2 * a.ncy, kPB, sm, st>>>(a);
+  bool narrow = false;
+  const cudaError_t e = push_narrow(sm, &narrow);
+  if (e != cudaSuccess) return e;
+  if (narrow)
+    k_push_deposit_narrow<<<2 * a.ncy, kPB, sm, st>>>(a);
+  else
+    k_push_deposit<<<2 * a.ncy, kPB, sm, st>>>(a);
   return cudaGetLastError();
 }
 
@@ -988,8 +1103,8 @@ cudaError_t push_batch(const SimArgs *inst, const int2 *row_work, int n, int max
 cudaError_t launch_push_deposit_batch(const SimArgs *inst, const int2 *row_work, int n, int max_nnx,
                                       int threads, cudaStream_t st) {
   if (n == 0) return cudaSuccess;
-  if (threads == 128) return push_batch<128>(inst, row_work, n, max_nnx, st);
-  return threads == 256 ? push_batch<256>(inst, row_work, n, max_nnx, st)
+  // 128 threads for rows of up to 64 cells, 512 for longer ones
+  return threads == 128 ? push_batch<128>(inst, row_work, n, max_nnx, st)
                         : push_batch<512>(inst, row_work, n, max_nnx, st);
 }
 
