@@ -578,9 +578,13 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
     float *S = src ? buf1 : buf0;
     float *D = src ? buf0 : buf1;
     // a solve with no tolerance that reports nothing (a correction of the
-    // precision form) needs no residual: no check, no grid barrier
-    const bool check = ((--to_check == 0) || (s == J.max_sweeps)) && (J.tol > 0.0 || J.write_stats);
-    if (to_check == 0) to_check = J.check_every;
+    // precision form) needs no residual: no check, no grid barrier.  A
+    // check before min_sweeps can stop nothing, and a later check replaces
+    // its residual, so those are skipped: a fixed-sweep solve (min = max)
+    // checks once, after its last sweep, with the same result and report.
+    const bool due = --to_check == 0;
+    if (due) to_check = J.check_every;
+    const bool check = ((due && s >= J.min_sweeps) || s == J.max_sweeps) && (J.tol > 0.0 || J.write_stats);
     m = (m >= K) ? 1 : m + 1;                        // position in the temporal block
     const int u0 = max(1, r0 - K + m) - lo;          // updated local rows [u0, u1)
     const int u1 = min(nny - 2, r1 - 1 + K - m) + 1 - lo;
