@@ -252,9 +252,9 @@ __device__ __forceinline__ float sweep_scalar(const float *__restrict__ S, float
 // strip's first and last rows (the neighbouring strips' south and north
 // rows) and, of the rows between, the values at the ends of a warp's span
 // and the seam columns -- every updated row in full only when `full` (the
-// sweep before a halo exchange).  Rows outside [u0, u1) keep their
-// registers unchanged, exactly as the shared-memory path leaves them
-// unwritten.
+// sweep before a halo exchange).  Halo rows outside the sweep's updated
+// range [u0, u1) are computed too (sweep_reg says why no updated row ever
+// reads them); the shared-memory path leaves them unwritten.
 struct RegGeom {
   int P, W, NG, gx, gy, lane, lr0, nvalid, col, lcol;
   bool active, lfix, rfix, seam;
@@ -266,10 +266,15 @@ template <int R, bool CHECK>
 __device__ __forceinline__ float sweep_reg(float4 (&x)[R], const float4 (&b)[R], const float *__restrict__ S,
                                            float *__restrict__ D, const RegGeom &g, int u0, int u1, int o0,
                                            int o1, bool full) {
-  // Straight-line code over the strip's rows: a row outside the strip or
-  // outside [u0, u1) computes from in-buffer addresses (row 0) and its
-  // result is discarded by selects and predicated stores, so the rows'
-  // independent chains can interleave.
+  // Straight-line code over the strip's rows, so the rows' independent
+  // chains can interleave: a row outside the strip computes from in-buffer
+  // addresses (row 0) and its result is discarded by selects and predicated
+  // stores.  Halo rows outside this sweep's updated range [u0, u1) are
+  // computed like the others: by the temporal block's shrinking range, a
+  // row outside it is read next only by rows outside the next sweep's
+  // range, and the exchange at the end of the block replaces every halo
+  // row (registers included), so their values never reach an updated row,
+  // and the range test and its selects are spared.
   const int P = g.P, W = g.W, col = g.col;
   const bool any = g.active && g.nvalid > 0;
   const float4 s4 = lds4(S + (any ? g.lr0 - 1 : 0) * P + col);
@@ -283,7 +288,6 @@ __device__ __forceinline__ float sweep_reg(float4 (&x)[R], const float4 (&b)[R],
     float rt = __shfl_down_sync(0xffffffffu, c.x, 1);
     const int lr = g.lr0 + r;
     const bool valid = g.active && r < g.nvalid;
-    const bool upd = valid && lr >= u0 && lr < u1;
     const float *rowp = S + (valid ? lr : 0) * P;
     if (g.lfix) lf = rowp[g.lcol];
     if (g.rfix) rt = rowp[col + 4];
@@ -295,18 +299,18 @@ __device__ __forceinline__ float sweep_reg(float4 (&x)[R], const float4 (&b)[R],
     v.w = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].w, c.z), rt), nb.w), prev.w));
     float *dp = D + (valid ? lr : 0) * P;
     const bool whole = full || r == 0 || r == g.nvalid - 1;
-    if (upd && whole) *reinterpret_cast<float4 *>(dp + col) = v;
-    if (upd && !whole && g.lfix) dp[col] = v.x;      // east neighbour of the lane before
-    if (upd && !whole && g.rfix) dp[col + 3] = v.w;  // west neighbour of the lane after (or of column 0)
-    if (upd && g.seam) dp[W] = v.x;
-    if (CHECK && upd && lr >= o0 && lr < o1) {
+    if (valid && whole) *reinterpret_cast<float4 *>(dp + col) = v;
+    if (valid && !whole && g.lfix) dp[col] = v.x;      // east neighbour of the lane before
+    if (valid && !whole && g.rfix) dp[col + 3] = v.w;  // west neighbour of the lane after (or of column 0)
+    if (valid && g.seam) dp[W] = v.x;
+    if (CHECK && valid && lr >= o0 && lr < o1) {
       md = fmaxf(md, fabsf(__fsub_rn(v.x, c.x)));
       md = fmaxf(md, fabsf(__fsub_rn(v.y, c.y)));
       md = fmaxf(md, fabsf(__fsub_rn(v.z, c.z)));
       md = fmaxf(md, fabsf(__fsub_rn(v.w, c.w)));
       if (g.seam) md = fmaxf(md, fabsf(__fsub_rn(v.x, rowp[W])));
     }
-    x[r] = upd ? v : c;
+    x[r] = valid ? v : c;
     prev = c;  // the previous value of row r is the south neighbour of row r+1
   }
   return md;
