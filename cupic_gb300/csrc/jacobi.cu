@@ -257,12 +257,14 @@ __device__ __forceinline__ float sweep_scalar(const float *__restrict__ S, float
 // reads them); the shared-memory path leaves them unwritten.
 struct RegGeom {
   int P, W, NG, gx, gy, lane, lr0, nvalid, col, lcol;
-  bool active, lfix, rfix, seam;
+  bool active, lfix, rfix, seam, whole_strip;
 };
 
 __device__ __forceinline__ float4 lds4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
 
-template <int R, bool CHECK>
+// FULL: the strip has all R rows (g.active and g.nvalid == R), known at
+// compile time, so no row needs a select.
+template <int R, bool CHECK, bool FULL = false>
 __device__ __forceinline__ float sweep_reg(float4 (&x)[R], const float4 (&b)[R], const float *__restrict__ S,
                                            float *__restrict__ D, const RegGeom &g, int u0, int u1, int o0,
                                            int o1, bool full) {
@@ -287,18 +289,18 @@ __device__ __forceinline__ float sweep_reg(float4 (&x)[R], const float4 (&b)[R],
     float lf = __shfl_up_sync(0xffffffffu, c.w, 1);
     float rt = __shfl_down_sync(0xffffffffu, c.x, 1);
     const int lr = g.lr0 + r;
-    const bool valid = g.active && r < g.nvalid;
+    const bool valid = FULL || (g.active && r < g.nvalid);
     const float *rowp = S + (valid ? lr : 0) * P;
     if (g.lfix) lf = rowp[g.lcol];
     if (g.rfix) rt = rowp[col + 4];
-    const float4 nb = (r + 1 < R && r + 1 < g.nvalid) ? x[r + 1 < R ? r + 1 : r] : n4;
+    const float4 nb = (r + 1 < R && (FULL || r + 1 < g.nvalid)) ? x[r + 1 < R ? r + 1 : r] : n4;
     float4 v;
     v.x = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].x, lf), c.y), nb.x), prev.x));
     v.y = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].y, c.x), c.z), nb.y), prev.y));
     v.z = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].z, c.y), c.w), nb.z), prev.z));
     v.w = __fmul_rn(0.25f, __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(b[r].w, c.z), rt), nb.w), prev.w));
     float *dp = D + (valid ? lr : 0) * P;
-    const bool whole = full || r == 0 || r == g.nvalid - 1;
+    const bool whole = full || r == 0 || r == (FULL ? R : g.nvalid) - 1;
     if (valid && whole) *reinterpret_cast<float4 *>(dp + col) = v;
     if (valid && !whole && g.lfix) dp[col] = v.x;      // east neighbour of the lane before
     if (valid && !whole && g.rfix) dp[col + 3] = v.w;  // west neighbour of the lane after (or of column 0)
@@ -474,6 +476,10 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
     rg.lr0 = 1 + rg.gy * R;
     rg.active = rg.lr0 < nrows - 1;
     rg.nvalid = rg.active ? min(R, nrows - 1 - rg.lr0) : 0;
+    // the same for every lane of a warp (its sweep shuffles across all 32):
+    // a warp whose lanes hold strips of different lengths takes the
+    // general form
+    rg.whole_strip = __all_sync(0xffffffffu, rg.active && rg.nvalid == R);
     rg.col = rg.gx << 2;
     rg.seam = rg.gx == 0;
     rg.lcol = rg.seam ? W - 1 : rg.col - 1;
@@ -491,8 +497,9 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
   }
   auto sweep = [&](const float *S, float *D, int u0, int u1, bool check, bool full) -> float {
     if constexpr (R > 0) {
-      return check ? sweep_reg<R, true>(x, bb, S, D, rg, u0, u1, o0, o1, full)
-                   : sweep_reg<R, false>(x, bb, S, D, rg, u0, u1, o0, o1, full);
+      if (check) return sweep_reg<R, true>(x, bb, S, D, rg, u0, u1, o0, o1, full);
+      return rg.whole_strip ? sweep_reg<R, false, true>(x, bb, S, D, rg, u0, u1, o0, o1, full)
+                            : sweep_reg<R, false>(x, bb, S, D, rg, u0, u1, o0, o1, full);
     } else {
       if (u0 >= u1) return 0.0f;
       // long segments walk up the columns; short ones (a few rows per
