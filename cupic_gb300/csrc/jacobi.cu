@@ -326,10 +326,18 @@ __device__ __forceinline__ float sweep_reg(float4 (&x)[R], const float4 (&b)[R],
 // and the neighbours trade their k boundary rows only every k sweeps.
 // R > 0 selects the register-strip sweep with strips of R rows; R == 0 the
 // shared-memory sweep (sweep_walk / sweep_vec / sweep_scalar).
+// the kernels' static shared scratch, one copy for every sweep form
+struct JScratch {
+  float red[33];                 // block_max
+  unsigned long long red64[33];  // block_max_u64
+  int bail;
+};
+
 template <int R>
 __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &J, const int c, float *jsm,
-                                            float *red, int *bail_p) {
-  int &bail = *bail_p;
+                                            JScratch *js) {
+  int &bail = js->bail;
+  float *const red = js->red;
   // uniform: flags of earlier kernels
   if (halted(a.ctl) || (J.gated && *reinterpret_cast<volatile int *>(&a.ctl->refine_done))) return;
   const int G = J.G, tid = threadIdx.x;
@@ -417,7 +425,7 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
   // a fused correction: the stop test of the solve on the grid's max |r|
   int chk0 = 0;  // rounds of the grid barrier counter used so far
   if (J.r64_phi) {
-    __shared__ unsigned long long red64[33];
+    unsigned long long *const red64 = js->red64;
     unsigned long long gm = block_max_u64((unsigned long long)__double_as_longlong(rmax), red64);
     if (G > 1) {
       // the CTAs' maxima in the residual slots, read back after a grid
@@ -534,19 +542,31 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
     const unsigned long long *hlo = J.halo + ((size_t)(e & 1) * G + (c - 1)) * 2 * K * P + K * P;
     const unsigned long long *hhi = J.halo + ((size_t)(e & 1) * G + (c + 1)) * 2 * K * P;
     bool ok = true;
-    for (int i = tid; i < nnx && ok; i += kJBlock) {
+    // A thread takes columns i and i + kJBlock together, all their loads in
+    // flight at once: with one column per pass, the thread that also held
+    // column 512 of a 513-node row polled twice in series, and every CTA
+    // waited for its second L2 round trip at every exchange.
+    const unsigned long long none = (unsigned long long)ep << 32;  // a word needing no wait
+    for (int i = tid; i < nnx && ok; i += 2 * kJBlock) {
+      const int i2 = i + kJBlock;
+      const bool two = i2 < nnx;
       for (int rb = 0; rb < K && ok; rb += kHaloBatch) {  // batches of rows per side, all loads in flight
-        unsigned long long wl[kHaloBatch], wh[kHaloBatch];
+        unsigned long long wl[kHaloBatch], wh[kHaloBatch], wl2[kHaloBatch], wh2[kHaloBatch];
         for (long long it = 0;; ++it) {
           bool all = true;
 #pragma unroll
           for (int q = 0; q < kHaloBatch; ++q) {
             const int r = rb + q;
-            wl[q] = (r < K && c > 0) ? ld_word(hlo + r * P + i) : ((unsigned long long)ep << 32);
-            wh[q] = (r < K && c < G - 1) ? ld_word(hhi + r * P + i) : ((unsigned long long)ep << 32);
+            const bool lo_ok = r < K && c > 0, hi_ok = r < K && c < G - 1;
+            wl[q] = lo_ok ? ld_word(hlo + r * P + i) : none;
+            wh[q] = hi_ok ? ld_word(hhi + r * P + i) : none;
+            wl2[q] = (two && lo_ok) ? ld_word(hlo + r * P + i2) : none;
+            wh2[q] = (two && hi_ok) ? ld_word(hhi + r * P + i2) : none;
           }
 #pragma unroll
-          for (int q = 0; q < kHaloBatch; ++q) all = all && (unsigned)(wl[q] >> 32) == ep && (unsigned)(wh[q] >> 32) == ep;
+          for (int q = 0; q < kHaloBatch; ++q)
+            all = all && (unsigned)(wl[q] >> 32) == ep && (unsigned)(wh[q] >> 32) == ep &&
+                  (unsigned)(wl2[q] >> 32) == ep && (unsigned)(wh2[q] >> 32) == ep;
           if (all) break;
           if (it >= kSpinLimit || ((it & 255) == 255 && *(volatile int *)&ctl->abort)) {
             ok = false;
@@ -559,8 +579,14 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
         for (int q = 0; q < kHaloBatch; ++q) {
           const int r = rb + q;
           // the lower neighbour's last K rows, the upper neighbour's first K rows
-          if (r < K && c > 0) D[(o0 - K + r) * P + i] = __uint_as_float((unsigned)wl[q]);
-          if (r < K && c < G - 1) D[(o1 + r) * P + i] = __uint_as_float((unsigned)wh[q]);
+          if (r < K && c > 0) {
+            D[(o0 - K + r) * P + i] = __uint_as_float((unsigned)wl[q]);
+            if (two) D[(o0 - K + r) * P + i2] = __uint_as_float((unsigned)wl2[q]);
+          }
+          if (r < K && c < G - 1) {
+            D[(o1 + r) * P + i] = __uint_as_float((unsigned)wh[q]);
+            if (two) D[(o1 + r) * P + i2] = __uint_as_float((unsigned)wh2[q]);
+          }
         }
       }
     }
@@ -717,27 +743,26 @@ __device__ __forceinline__ void jacobi_body(const SimArgs &a, const JacobiArgs &
 }
 
 __device__ __forceinline__ void jacobi_dispatch(const SimArgs &a, const JacobiArgs &J, int c, float *jsm,
-                                                float *red, int *bail) {
+                                                JScratch *js) {
   switch (J.strip) {
-    case 1: jacobi_body<1>(a, J, c, jsm, red, bail); break;
-    case 2: jacobi_body<2>(a, J, c, jsm, red, bail); break;
-    case 3: jacobi_body<3>(a, J, c, jsm, red, bail); break;
-    case 4: jacobi_body<4>(a, J, c, jsm, red, bail); break;
-    case 5: jacobi_body<5>(a, J, c, jsm, red, bail); break;
-    case 6: jacobi_body<6>(a, J, c, jsm, red, bail); break;
-    case 7: jacobi_body<7>(a, J, c, jsm, red, bail); break;
-    case 8: jacobi_body<8>(a, J, c, jsm, red, bail); break;
-    default: jacobi_body<0>(a, J, c, jsm, red, bail); break;
+    case 1: jacobi_body<1>(a, J, c, jsm, js); break;
+    case 2: jacobi_body<2>(a, J, c, jsm, js); break;
+    case 3: jacobi_body<3>(a, J, c, jsm, js); break;
+    case 4: jacobi_body<4>(a, J, c, jsm, js); break;
+    case 5: jacobi_body<5>(a, J, c, jsm, js); break;
+    case 6: jacobi_body<6>(a, J, c, jsm, js); break;
+    case 7: jacobi_body<7>(a, J, c, jsm, js); break;
+    case 8: jacobi_body<8>(a, J, c, jsm, js); break;
+    default: jacobi_body<0>(a, J, c, jsm, js); break;
   }
 }
 
 __global__ void __launch_bounds__(kJBlock, 1) k_jacobi(SimArgs a, JacobiArgs J) {
   extern __shared__ __align__(16) float jsm[];
-  __shared__ float red[33];
-  __shared__ int bail;
-  if (threadIdx.x == 0) bail = 0;
+  __shared__ JScratch js;
+  if (threadIdx.x == 0) js.bail = 0;
   __syncthreads();
-  jacobi_dispatch(a, J, blockIdx.x, jsm, red, &bail);
+  jacobi_dispatch(a, J, blockIdx.x, jsm, &js);
 }
 
 // Many contexts' solves in one cooperative launch.  The grid is split into
@@ -749,8 +774,7 @@ __global__ void __launch_bounds__(kJBlock, 1)
     k_jacobi_batch(const SimArgs *__restrict__ inst, const JacobiArgs *__restrict__ jargs,
                    const JGroup *__restrict__ groups, int ngroups, const int *__restrict__ list) {
   extern __shared__ __align__(16) float jsm[];
-  __shared__ float red[33];
-  __shared__ int bail;
+  __shared__ JScratch js;
   int g = 0;
   while (g + 1 < ngroups && groups[g + 1].first <= (int)blockIdx.x) ++g;
   const JGroup gr = groups[g];
@@ -758,9 +782,9 @@ __global__ void __launch_bounds__(kJBlock, 1)
   if (c < 0 || c >= gr.G) return;
   for (int q = gr.begin; q < gr.end; ++q) {
     const int i = list[q];
-    if (threadIdx.x == 0) bail = 0;
+    if (threadIdx.x == 0) js.bail = 0;
     __syncthreads();
-    jacobi_dispatch(inst[i], jargs[i], c, jsm, red, &bail);
+    jacobi_dispatch(inst[i], jargs[i], c, jsm, &js);
     __syncthreads();
   }
 }
