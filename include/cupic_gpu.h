@@ -80,7 +80,9 @@ typedef struct cupic_params {
   /* Jacobi control for each step (main.cu:64; mesh.cu:94-114).  A sweep
    * count s stops the solve when s >= min_sweeps and the max |delta phi| of
    * a checked sweep is < tol, or when s == max_sweeps.  A sweep is checked
-   * when s % check_every == 0 or s == max_sweeps. */
+   * when s % check_every == 0 or s == max_sweeps; the reported residual is
+   * that of the last checked sweep.  (Checks before min_sweeps, which can
+   * stop nothing, are not computed; the stop and the report are the same.) */
   double tol;
   int32_t min_sweeps, max_sweeps, check_every;
   /* the same for the initial solve (init.cu:254) */

@@ -118,6 +118,40 @@ def test_repeated_short_solves_match_oracle(make_pair, monkeypatch):
         np.testing.assert_array_equal(sim.phi().astype(np.float64), ora.phi(), err_msg=f"{n} sweeps")
 
 
+@pytest.mark.parametrize("tol,mn,mx,chk", [(1e-30, 30, 30, 1), (2e-3, 25, 400, 1),
+                                             (2e-3, 25, 400, 7), (5e-4, 40, 600, 3)])
+def test_solve_stop_rule_matches_oracle(make_pair, tol, mn, mx, chk):
+    """The stop rule (mesh.cu:94-114 with min/max sweeps and a check every
+    chk sweeps): the sweep count, the reported residual and the potential
+    are the oracle's, which checks from the first sweep; the GPU skips the
+    checks before min_sweeps, which can stop nothing.  Bit-exact: the
+    oracle stops at sweeps 30, 25, 28 and 195 on these cases."""
+    import ctypes
+    torch = pytest.importorskip("torch")
+    sim, ora = make_pair("small", ctas=4)
+    sim.init_plasma()
+    ora.init_plasma()
+    p = sim.p
+    rho = np.ascontiguousarray(sim.rho_fixed(0).ravel(), dtype=np.int64)
+    phi0 = np.ascontiguousarray(sim.phi().ravel(), dtype=np.float32)
+    sw_o, res_o = ora.solve(tol, mn, mx, chk)
+    # the allocation-free entry point reports the sweeps and the residual
+    L = cg.load_library()
+    d_rho = torch.from_numpy(rho).to("cuda")
+    d_phi = torch.from_numpy(phi0.copy()).to("cuda")
+    torch.cuda.synchronize()
+    sweeps, res = ctypes.c_int32(), ctypes.c_float()
+    rc = L.cupic_poisson_solver_static(ctypes.byref(p), d_rho.data_ptr(), d_phi.data_ptr(), None, tol,
+                                       mn, mx, chk, None, ctypes.byref(sweeps), ctypes.byref(res))
+    assert rc == 0, cg.strerror(rc)
+    assert sweeps.value == sw_o
+    assert res.value == np.float32(res_o)
+    np.testing.assert_array_equal(d_phi.cpu().numpy().astype(np.float64), ora.phi().ravel())
+    # and the context's solver on the same state
+    sim.poisson_solver(tol, mn, mx, chk)
+    np.testing.assert_array_equal(sim.phi().astype(np.float64), ora.phi())
+
+
 def test_stage_api_matches_oracle(make_pair):
     """Drive the reference's entry points one by one on a state loaded from
     host arrays (read_particle_file + the main loop, main.cu:59-96)."""
